@@ -1,0 +1,141 @@
+/*
+ * nr_ldpc_gb300 -- GB300 (sm_103a) 5G NR / QC-LDPC normalized min-sum decoder.
+ *
+ * C ABI: plain pointers and sizes, no C++ or framework types.  Every entry
+ * point returns an nrldpc_status (0 = OK, negative = error) and never exits
+ * the process.  Calls taking a cudaStream_t are stream-ordered and
+ * asynchronous unless documented otherwise; the caller synchronizes.
+ *
+ * Reference interfaces replaced (ctarver/NR_GPU_LDPC):
+ *   nrldpc_setup_ldpc      <- ldpc_params setup_ldpc(int, float, int)       src/nr_ldpc.h:14,
+ *                                                                           src/nr_ldpc.cpp:31-230
+ *   nrldpc_init            <- setup_dev_memory + setup_gpu_grid +
+ *                             put_h_compact_and_params_in_constant_memory   src/setup_exp.h:16-30,
+ *                                                                           src/setup_exp.cu:102-166,286-313
+ *   nrldpc_destroy         <- (none: the reference never frees its device memory)
+ *   nrldpc_decode          <- perform_gpu_ldpc_decoding<T>, decode part     src/gpu_decoder_top.h:13-18,
+ *                             (device LLR in, device packed bits out)       src/gpu_decoder_top.cu:25-49
+ *   nrldpc_decode_host_async <- perform_gpu_ldpc_decoding<T>, whole call:   src/gpu_decoder_top.cu:16-52
+ *                             H2D of the LLR batch, decode, D2H of packed
+ *                             hard decisions, all queued on one stream
+ *                             (src/cuda_gpu_wrapper/gpu_setup.cu:75-97)
+ *
+ * Data formats (identical to the reference where it defines them):
+ *   LLR      fp32 [n_cw][cols*Z], codeword-bit order, positive = bit 0; the
+ *            punctured first 2Z columns carry LLR 0 (src/encoding_tools.cpp:85-99).
+ *   packed   uint8 [n_cw][ceil(cols*Z/8)]: bit i of byte b is the hard
+ *            decision of column 8b+i (1 when the posterior is not > 0),
+ *            src/ldpc_kernels.cu:463-467,482-500, src/host_helpers.cpp:60-64.
+ *            For Z % 8 == 0 this is byte-identical to the reference stream.
+ */
+#ifndef NR_LDPC_GB300_H
+#define NR_LDPC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* nrldpc_stream_t; /* same object as cudaStream_t */
+typedef struct nrldpc_handle nrldpc_handle;
+
+typedef enum {
+    NRLDPC_OK = 0,
+    NRLDPC_ERR_INVALID_ARG = -1,   /* null pointer, negative count, bad option */
+    NRLDPC_ERR_BAD_CONFIG = -2,    /* unsupported base graph / lifting size */
+    NRLDPC_ERR_CUDA = -3,          /* a CUDA runtime call or launch failed */
+    NRLDPC_ERR_ALIGNMENT = -4,     /* device LLR pointer not 16-byte aligned */
+    NRLDPC_ERR_TOO_LARGE = -5,     /* batch beyond the handle's max_batch */
+    NRLDPC_ERR_TIMEOUT = -6,       /* a bounded device-side wait expired */
+    NRLDPC_ERR_NO_MEMORY = -7,     /* host or device allocation failed */
+    NRLDPC_ERR_NO_DEVICE = -8      /* no CUDA device / wrong architecture */
+} nrldpc_status;
+
+/* Code parameters as the reference computes them (mirror of ldpc_params,
+ * src/types.h:38-55; pointer members replaced by the iLS index). */
+typedef struct {
+    int A, bg_index, Z, K, N, H_rows, H_cols, n_nz_in_row, n_nz_in_col;
+    int n_iterations, N_before_puncture, i_ls, C, K_b;
+    float rate;
+} nrldpc_ldpc_params;
+
+/* Host-only; no GPU needed.  Same selection rules (and quirks) as the
+ * reference's setup_ldpc.  Returns NRLDPC_ERR_BAD_CONFIG where the
+ * reference would read an uninitialized set index. */
+int nrldpc_setup_ldpc(int A, float rate, int n_iterations, nrldpc_ldpc_params* out);
+
+/* Lifting-size set index of Z (TS 38.212 Table 5.3.2-1), or -1. */
+int nrldpc_set_index(int z);
+
+/* Dense base matrix of (bg, iLS) into out[rows*cols] (-1 = zero block,
+ * unreduced shifts).  Host-only.  rows/cols may be NULL. */
+int nrldpc_base_matrix(int bg, int ils, int* out, int* rows, int* cols);
+
+typedef struct {
+    int bg;          /* 1 or 2; 0 = custom base matrix (nrldpc_init_custom) */
+    int z;           /* lifting size */
+    int max_batch;   /* largest n_cw of one decode call */
+    float alpha;     /* normalization; the reference hard-codes 0.75 */
+    int device;      /* CUDA device ordinal */
+    int cw_per_cta;  /* codewords per CTA; 0 = tuned default */
+} nrldpc_config;
+
+int nrldpc_init(const nrldpc_config* cfg, nrldpc_handle** out);
+/* Custom QC base matrix (rows <= 46, cols <= 68, row degree <= 19), e.g.
+ * the 802.11n 12x24 matrix.  Shifts are reduced mod z. */
+int nrldpc_init_custom(const int* base, int rows, int cols, const nrldpc_config* cfg,
+                       nrldpc_handle** out);
+int nrldpc_destroy(nrldpc_handle* h);
+
+/* Code geometry of a handle (any pointer may be NULL). */
+int nrldpc_geometry(const nrldpc_handle* h, int* rows, int* cols, int* z, int* n_edges,
+                    int* n_bp, int* packed_bytes);
+
+/* Decode n_cw codewords for n_iter iterations (device pointers).
+ *   d_llr     [n_cw][n_bp] fp32, 16-byte aligned
+ *   d_packed  [n_cw][packed_bytes]
+ *   d_app     NULL or [n_cw][n_bp] fp32: posterior of the iteration decided on
+ *   d_iters   NULL or [n_cw] int32: iterations after which the decision was taken
+ *   early_stop  0: fixed n_iter (reference behaviour); 1: stop a codeword once
+ *               its hard decisions satisfy every parity check. */
+int nrldpc_decode(nrldpc_handle* h, const float* d_llr, uint8_t* d_packed, int n_cw, int n_iter,
+                  int early_stop, float* d_app, int32_t* d_iters, nrldpc_stream_t stream);
+
+/* Host buffers (pinned for overlap, pageable works): H2D into the handle's
+ * staging, decode, D2H -- queued on `stream`, returns without waiting. */
+int nrldpc_decode_host_async(nrldpc_handle* h, const float* h_llr, uint8_t* h_packed, int n_cw,
+                             int n_iter, int early_stop, nrldpc_stream_t stream);
+
+/* Learned weighted min-sum: per (iteration, base edge) scale factors
+ * w[n_w_iters][n_edges] replacing alpha (iterations past n_w_iters reuse the
+ * last row).  Host pointer; copied into the handle.  n_w_iters = 0 clears. */
+int nrldpc_set_weights(nrldpc_handle* h, const float* w, int n_w_iters);
+/* As nrldpc_decode, with the weights set on the handle. */
+int nrldpc_decode_weighted(nrldpc_handle* h, const float* d_llr, uint8_t* d_packed, int n_cw,
+                           int n_iter, int early_stop, float* d_app, int32_t* d_iters,
+                           nrldpc_stream_t stream);
+
+/* Seeded channel generator on the GPU (bit-identical to the CPU oracle's):
+ * info bits (Philox4x32-10), encode, BPSK, AWGN sigma[i], LLR = 2y/sigma^2;
+ * first n_punct_cols columns get LLR 0.  d_cw_packed may be NULL. */
+int nrldpc_gen_llr(nrldpc_handle* h, uint64_t seed, uint64_t cw_base, int n_cw,
+                   const float* d_sigma, int n_punct_cols, float* d_llr, uint8_t* d_cw_packed,
+                   nrldpc_stream_t stream);
+
+/* Count info-bit errors of decoded vs transmitted packed words over the
+ * first n_info bits: d_counts[2] += {bit errors, frame errors}. */
+int nrldpc_count_errors(nrldpc_handle* h, const uint8_t* d_packed, const uint8_t* d_cw_packed,
+                        int n_cw, int n_info, unsigned long long* d_counts,
+                        nrldpc_stream_t stream);
+
+/* Last device-side error recorded by a bounded wait (0 if none); clears it. */
+int nrldpc_device_error(nrldpc_handle* h);
+
+const char* nrldpc_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,426 @@
+// C-ABI of the decoder (include/nr_ldpc_gb300.h): code setup, handles,
+// device buffers and launches.  Host code only; kernels live in decode.cu
+// and channel.cu.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/nr_ldpc_gb300.h"
+#include "nrldpc_internal.h"
+
+using namespace nrldpc;
+
+namespace {
+#include "base_graphs.inc"
+
+const int kBaseZ[8] = {2, 3, 5, 7, 9, 11, 13, 15};
+
+struct Handle {
+    int device = 0;
+    CodeTable tab{};
+    EncodePlan plan{};
+    bool plan_ok = false;
+    float alpha = 0.75f;
+    int max_batch = 0;
+    int cpb = 1, threads = 32, ctas_per_sm = 1, sm_count = 1, max_grid = 1, minb = 1;
+    size_t smem = 0;
+    uint4* state = nullptr;
+    int* scratch = nullptr;  // [0] work counter, [1] error flag
+    float* stage_llr = nullptr;
+    uint8_t* stage_packed = nullptr;
+    float* weights = nullptr;
+    int n_w_iters = 0;
+};
+
+int map_cuda(cudaError_t e) { return e == cudaSuccess ? NRLDPC_OK : NRLDPC_ERR_CUDA; }
+
+bool fill_table(const int* base, int rows, int cols, int z, int kb, CodeTable* t) {
+    if (rows < 1 || rows > kMaxRows || cols < 1 || cols > kMaxCols || z < 1 || z > kMaxZ) return false;
+    // n_bp % 4 == 0: whole float4 / 16-byte bulk copies of a codeword
+    if (cols * z > 0xffff || (cols * z) % 4 != 0) return false;
+    std::memset(t, 0, sizeof(*t));
+    t->rows = rows;
+    t->cols = cols;
+    t->z = z;
+    t->n_bp = cols * z;
+    t->packed_bytes = (t->n_bp + 7) / 8;
+    t->kb = kb;
+    int e = 0;
+    for (int r = 0; r < rows; r++) {
+        t->row_ptr[r] = static_cast<uint16_t>(e);
+        int deg = 0;
+        for (int c = 0; c < cols; c++) {
+            const int v = base[r * cols + c];
+            if (v == -1) continue;
+            if (v < 0 || e >= kMaxEdges) return false;
+            const int sh = v % z;
+            t->edge[e] = static_cast<uint32_t>(c * z + sh) | (static_cast<uint32_t>(z - sh) << 16);
+            t->edge_col[e] = static_cast<uint8_t>(c);
+            t->edge_shift[e] = static_cast<uint16_t>(sh);
+            e++;
+            deg++;
+        }
+        if (deg < 1 || deg > kMaxDeg) return false;
+        t->row_deg[r] = static_cast<uint8_t>(deg);
+    }
+    t->row_ptr[rows] = static_cast<uint16_t>(e);
+    t->n_edges = e;
+    // Barrier placement: greedy groups of consecutive rows that pairwise share
+    // no base column; a barrier closes each group.
+    std::vector<int> used(cols, 0);
+    for (int r = 0; r < rows; r++) {
+        bool clash = false;
+        for (int k = t->row_ptr[r]; k < t->row_ptr[r + 1]; k++) clash |= used[t->edge_col[k]] != 0;
+        if (clash) {
+            t->sync_after[r - 1] = 1;
+            std::fill(used.begin(), used.end(), 0);
+        }
+        for (int k = t->row_ptr[r]; k < t->row_ptr[r + 1]; k++) used[t->edge_col[k]] = 1;
+    }
+    t->sync_after[rows - 1] = 1;
+    return true;
+}
+
+int base_matrix_impl(int bg, int ils, int* out, int* rows, int* cols) {
+    if ((bg != 1 && bg != 2) || ils < 0 || ils > 7) return NRLDPC_ERR_BAD_CONFIG;
+    const int R = bg == 1 ? 46 : 42, C = bg == 1 ? 68 : 52;
+    if (rows) *rows = R;
+    if (cols) *cols = C;
+    if (!out) return NRLDPC_OK;
+    for (int i = 0; i < R * C; i++) out[i] = -1;
+    const int n = bg == 1 ? NRLDPC_BG1_EDGES : NRLDPC_BG2_EDGES;
+    for (int k = 0; k < n; k++) {
+        if (bg == 1)
+            out[kBg1Row[k] * C + kBg1Col[k]] = kBg1Shift[k][ils];
+        else
+            out[kBg2Row[k] * C + kBg2Col[k]] = kBg2Shift[k][ils];
+    }
+    return NRLDPC_OK;
+}
+
+void free_handle(Handle* h) {
+    if (!h) return;
+    cudaFree(h->state);
+    cudaFree(h->scratch);
+    cudaFree(h->stage_llr);
+    cudaFree(h->stage_packed);
+    cudaFree(h->weights);
+    delete h;
+}
+
+int init_impl(const int* base, int rows, int cols, int kb, const nrldpc_config* cfg,
+              nrldpc_handle** out) {
+    if (!cfg || !out || cfg->max_batch < 1 || !(cfg->alpha > 0.0f) || cfg->cw_per_cta < 0)
+        return NRLDPC_ERR_INVALID_ARG;
+    *out = nullptr;
+    Handle* h = new (std::nothrow) Handle();
+    if (!h) return NRLDPC_ERR_NO_MEMORY;
+    if (!fill_table(base, rows, cols, cfg->z, kb, &h->tab)) {
+        delete h;
+        return NRLDPC_ERR_BAD_CONFIG;
+    }
+    h->plan_ok = make_encode_plan(h->tab, &h->plan);
+    h->device = cfg->device;
+    h->alpha = cfg->alpha;
+    h->max_batch = cfg->max_batch;
+    int n_dev = 0;
+    if (cudaGetDeviceCount(&n_dev) != cudaSuccess || cfg->device < 0 || cfg->device >= n_dev) {
+        delete h;
+        return NRLDPC_ERR_NO_DEVICE;
+    }
+    cudaSetDevice(cfg->device);
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, cfg->device) != cudaSuccess) {
+        delete h;
+        return NRLDPC_ERR_NO_DEVICE;
+    }
+    h->sm_count = prop.multiProcessorCount;
+    const size_t smem_limit = prop.sharedMemPerBlockOptin;
+    const int z = cfg->z;
+    int cpb = cfg->cw_per_cta;
+    if (cpb == 0) {
+        cpb = std::max(1, kMaxThreads / z);
+        while (cpb > 1 && decode_smem_bytes(h->tab, cpb) > smem_limit) cpb--;
+        cpb = std::min(cpb, 48);
+    }
+    if (cpb * z > kMaxThreads || decode_smem_bytes(h->tab, cpb) > smem_limit || cpb > 48) {
+        delete h;
+        return NRLDPC_ERR_BAD_CONFIG;
+    }
+    h->cpb = cpb;
+    h->threads = (cpb * z + 31) / 32 * 32;
+    h->smem = decode_smem_bytes(h->tab, cpb);
+    // opt in to the device maximum once, so handles of any size can coexist
+    if (map_cuda(decode_kernel_attributes(smem_limit))) {
+        delete h;
+        return NRLDPC_ERR_CUDA;
+    }
+    // one CTA per SM by shared memory -> give it the full register budget
+    h->minb = (2 * (h->smem + 1024) <= prop.sharedMemPerMultiprocessor) ? 2 : 1;
+    h->ctas_per_sm = std::max(1, std::min(decode_max_ctas_per_sm(false, h->minb, h->threads, h->smem),
+                                          decode_max_ctas_per_sm(true, h->minb, h->threads, h->smem)));
+    h->max_grid = h->ctas_per_sm * h->sm_count;
+    const size_t state_elems =
+        static_cast<size_t>(h->max_grid) * cpb * h->tab.rows * static_cast<size_t>(z);
+    const size_t n_llr = static_cast<size_t>(cfg->max_batch) * h->tab.n_bp;
+    if (cudaMalloc(&h->state, state_elems * sizeof(uint4)) != cudaSuccess ||
+        cudaMalloc(&h->scratch, 64) != cudaSuccess || cudaMemset(h->scratch, 0, 64) != cudaSuccess ||
+        cudaMalloc(&h->stage_llr, n_llr * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&h->stage_packed,
+                   static_cast<size_t>(cfg->max_batch) * h->tab.packed_bytes) != cudaSuccess) {
+        free_handle(h);
+        return NRLDPC_ERR_NO_MEMORY;
+    }
+    *out = reinterpret_cast<nrldpc_handle*>(h);
+    return NRLDPC_OK;
+}
+
+int decode_impl(Handle* h, const float* llr, uint8_t* packed, int n_cw, int n_iter, int early,
+                float* app, int32_t* iters, bool weighted, cudaStream_t stream) {
+    if (!h || !llr || !packed || n_cw < 0 || n_iter < 1 || (early != 0 && early != 1))
+        return NRLDPC_ERR_INVALID_ARG;
+    if (n_cw == 0) return NRLDPC_OK;
+    if (n_cw > h->max_batch) return NRLDPC_ERR_TOO_LARGE;
+    if (reinterpret_cast<uintptr_t>(llr) % 16 != 0) return NRLDPC_ERR_ALIGNMENT;
+    if (weighted && (!h->weights || h->n_w_iters < 1)) return NRLDPC_ERR_INVALID_ARG;
+    DecodeArgs a{};
+    a.llr = llr;
+    a.packed = packed;
+    a.app = app;
+    a.iters = iters;
+    a.state = h->state;
+    a.work_counter = h->scratch;
+    a.error_flag = h->scratch + 1;
+    a.weights = weighted ? h->weights : nullptr;
+    a.n_cw = n_cw;
+    a.n_iter = n_iter;
+    a.cpb = h->cpb;
+    a.n_groups = (n_cw + h->cpb - 1) / h->cpb;
+    a.n_w_iters = h->n_w_iters;
+    a.early_stop = early;
+    a.alpha = h->alpha;
+    const int grid = std::min(a.n_groups, h->max_grid);
+    cudaError_t e = cudaMemsetAsync(h->scratch, 0, sizeof(int), stream);
+    if (e != cudaSuccess) return NRLDPC_ERR_CUDA;
+    return map_cuda(launch_decode(h->tab, a, grid, h->threads, h->smem, weighted, h->minb, stream));
+}
+
+}  // namespace
+
+extern "C" {
+
+int nrldpc_set_index(int z) {
+    for (int i = 0; i < 8; i++)
+        for (int v = kBaseZ[i]; v <= 384; v *= 2)
+            if (v == z) return i;
+    return -1;
+}
+
+int nrldpc_base_matrix(int bg, int ils, int* out, int* rows, int* cols) {
+    return base_matrix_impl(bg, ils, out, rows, cols);
+}
+
+// Mirror of setup_ldpc (src/nr_ldpc.cpp:31-230), quirks included.
+int nrldpc_setup_ldpc(int A, float rate, int n_iterations, nrldpc_ldpc_params* o) {
+    if (!o) return NRLDPC_ERR_INVALID_ARG;
+    const int l = (A > 3824) ? 24 : 16;
+    const int B = A + l;
+    int bg, k_cb, k_b;
+    if ((A <= 292) || (A < 3824 && rate <= 0.67) || (rate <= 0.25)) {
+        bg = 2;
+        k_cb = 3840;
+        k_b = B > 640 ? 10 : B > 560 ? 9 : B > 192 ? 8 : 6;
+    } else {
+        bg = 1;
+        k_cb = 8448;
+        k_b = 22;
+    }
+    int C, b_prime;
+    if (B <= k_cb) {
+        C = 1;
+        b_prime = B;
+    } else {
+        C = B / (k_cb - 24);  // ceil() of an integer quotient, as the reference
+        b_prime = B + C * 24;
+    }
+    const int k_prime = b_prime / C;
+    const int z_min = k_prime / k_b;
+    int z_c = 1000, i_ls = -1;
+    for (int i = 0; i < 8; i++) {
+        int t = kBaseZ[i];
+        for (int k = 0; k < 8; k++) {
+            const int v = t < 385 ? t : 0;
+            t *= 2;
+            if (v >= z_min && v < z_c) {
+                z_c = v;
+                i_ls = i;
+            }
+        }
+    }
+    if (i_ls < 0) return NRLDPC_ERR_BAD_CONFIG;
+    std::memset(o, 0, sizeof(*o));
+    o->A = A;
+    o->rate = rate;
+    o->bg_index = bg;
+    o->Z = z_c;
+    o->K = bg == 1 ? 22 * z_c : 10 * z_c;
+    o->N = bg == 1 ? 66 * z_c : 50 * z_c;
+    o->H_rows = bg == 1 ? 46 : 42;
+    o->H_cols = bg == 1 ? 68 : 52;
+    std::vector<int> H(o->H_rows * o->H_cols);
+    base_matrix_impl(bg, i_ls, H.data(), nullptr, nullptr);
+    int mr = 0, mc = 0;
+    for (int r = 0; r < o->H_rows; r++) {
+        int c = 0;
+        for (int j = 0; j < o->H_cols; j++) c += H[r * o->H_cols + j] != -1;
+        mr = std::max(mr, c);
+    }
+    for (int j = 0; j < o->H_cols; j++) {
+        int c = 0;
+        for (int r = 0; r < o->H_rows; r++) c += H[r * o->H_cols + j] != -1;
+        mc = std::max(mc, c);
+    }
+    o->n_nz_in_row = mr;
+    o->n_nz_in_col = mc;
+    o->n_iterations = n_iterations;
+    o->N_before_puncture = o->N + 2 * z_c;
+    o->i_ls = i_ls;
+    o->C = C;
+    o->K_b = k_b;
+    return NRLDPC_OK;
+}
+
+int nrldpc_init(const nrldpc_config* cfg, nrldpc_handle** out) {
+    if (!cfg || !out) return NRLDPC_ERR_INVALID_ARG;
+    const int ils = nrldpc_set_index(cfg->z);
+    if ((cfg->bg != 1 && cfg->bg != 2) || ils < 0) return NRLDPC_ERR_BAD_CONFIG;
+    int rows = 0, cols = 0;
+    std::vector<int> H(46 * 68);
+    base_matrix_impl(cfg->bg, ils, H.data(), &rows, &cols);
+    return init_impl(H.data(), rows, cols, cfg->bg == 1 ? 22 : 10, cfg, out);
+}
+
+int nrldpc_init_custom(const int* base, int rows, int cols, const nrldpc_config* cfg,
+                       nrldpc_handle** out) {
+    if (!base || !cfg || !out) return NRLDPC_ERR_INVALID_ARG;
+    // systematic columns: everything before the first column of the parity staircase
+    return init_impl(base, rows, cols, cols - rows, cfg, out);
+}
+
+int nrldpc_destroy(nrldpc_handle* handle) {
+    free_handle(reinterpret_cast<Handle*>(handle));
+    return NRLDPC_OK;
+}
+
+int nrldpc_geometry(const nrldpc_handle* handle, int* rows, int* cols, int* z, int* n_edges,
+                    int* n_bp, int* packed_bytes) {
+    const Handle* h = reinterpret_cast<const Handle*>(handle);
+    if (!h) return NRLDPC_ERR_INVALID_ARG;
+    if (rows) *rows = h->tab.rows;
+    if (cols) *cols = h->tab.cols;
+    if (z) *z = h->tab.z;
+    if (n_edges) *n_edges = h->tab.n_edges;
+    if (n_bp) *n_bp = h->tab.n_bp;
+    if (packed_bytes) *packed_bytes = h->tab.packed_bytes;
+    return NRLDPC_OK;
+}
+
+int nrldpc_decode(nrldpc_handle* handle, const float* d_llr, uint8_t* d_packed, int n_cw,
+                  int n_iter, int early_stop, float* d_app, int32_t* d_iters,
+                  nrldpc_stream_t stream) {
+    return decode_impl(reinterpret_cast<Handle*>(handle), d_llr, d_packed, n_cw, n_iter, early_stop,
+                       d_app, d_iters, false, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int nrldpc_decode_weighted(nrldpc_handle* handle, const float* d_llr, uint8_t* d_packed, int n_cw,
+                           int n_iter, int early_stop, float* d_app, int32_t* d_iters,
+                           nrldpc_stream_t stream) {
+    return decode_impl(reinterpret_cast<Handle*>(handle), d_llr, d_packed, n_cw, n_iter, early_stop,
+                       d_app, d_iters, true, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int nrldpc_decode_host_async(nrldpc_handle* handle, const float* h_llr, uint8_t* h_packed,
+                             int n_cw, int n_iter, int early_stop, nrldpc_stream_t stream) {
+    Handle* h = reinterpret_cast<Handle*>(handle);
+    if (!h || !h_llr || !h_packed || n_cw < 0) return NRLDPC_ERR_INVALID_ARG;
+    if (n_cw > h->max_batch) return NRLDPC_ERR_TOO_LARGE;
+    if (n_cw == 0) return NRLDPC_OK;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const size_t in_bytes = static_cast<size_t>(n_cw) * h->tab.n_bp * sizeof(float);
+    const size_t out_bytes = static_cast<size_t>(n_cw) * h->tab.packed_bytes;
+    if (cudaMemcpyAsync(h->stage_llr, h_llr, in_bytes, cudaMemcpyHostToDevice, s) != cudaSuccess)
+        return NRLDPC_ERR_CUDA;
+    const int rc = decode_impl(h, h->stage_llr, h->stage_packed, n_cw, n_iter, early_stop, nullptr,
+                               nullptr, false, s);
+    if (rc) return rc;
+    return map_cuda(cudaMemcpyAsync(h_packed, h->stage_packed, out_bytes, cudaMemcpyDeviceToHost, s));
+}
+
+int nrldpc_set_weights(nrldpc_handle* handle, const float* w, int n_w_iters) {
+    Handle* h = reinterpret_cast<Handle*>(handle);
+    if (!h || n_w_iters < 0 || (n_w_iters > 0 && !w)) return NRLDPC_ERR_INVALID_ARG;
+    cudaFree(h->weights);
+    h->weights = nullptr;
+    h->n_w_iters = 0;
+    if (n_w_iters == 0) return NRLDPC_OK;
+    const size_t bytes = static_cast<size_t>(n_w_iters) * h->tab.n_edges * sizeof(float);
+    if (cudaMalloc(&h->weights, bytes) != cudaSuccess) return NRLDPC_ERR_NO_MEMORY;
+    if (cudaMemcpy(h->weights, w, bytes, cudaMemcpyHostToDevice) != cudaSuccess) return NRLDPC_ERR_CUDA;
+    h->n_w_iters = n_w_iters;
+    return NRLDPC_OK;
+}
+
+int nrldpc_gen_llr(nrldpc_handle* handle, uint64_t seed, uint64_t cw_base, int n_cw,
+                   const float* d_sigma, int n_punct_cols, float* d_llr, uint8_t* d_cw_packed,
+                   nrldpc_stream_t stream) {
+    Handle* h = reinterpret_cast<Handle*>(handle);
+    if (!h || !d_sigma || !d_llr || n_cw < 0 || n_punct_cols < 0 || n_punct_cols > h->tab.cols)
+        return NRLDPC_ERR_INVALID_ARG;
+    if (!h->plan_ok) return NRLDPC_ERR_BAD_CONFIG;
+    if (n_cw == 0) return NRLDPC_OK;
+    return map_cuda(launch_gen_llr(h->tab, h->plan, seed, cw_base, n_cw, d_sigma, n_punct_cols, d_llr,
+                                   d_cw_packed, reinterpret_cast<cudaStream_t>(stream)));
+}
+
+int nrldpc_count_errors(nrldpc_handle* handle, const uint8_t* d_packed, const uint8_t* d_cw_packed,
+                        int n_cw, int n_info, unsigned long long* d_counts, nrldpc_stream_t stream) {
+    Handle* h = reinterpret_cast<Handle*>(handle);
+    if (!h || !d_packed || !d_cw_packed || !d_counts || n_cw < 0 || n_info < 0 ||
+        n_info > h->tab.n_bp)
+        return NRLDPC_ERR_INVALID_ARG;
+    if (n_cw == 0) return NRLDPC_OK;
+    return map_cuda(launch_count_errors(d_packed, d_cw_packed, n_cw, h->tab.packed_bytes, n_info,
+                                        d_counts, reinterpret_cast<cudaStream_t>(stream)));
+}
+
+int nrldpc_device_error(nrldpc_handle* handle) {
+    Handle* h = reinterpret_cast<Handle*>(handle);
+    if (!h) return NRLDPC_ERR_INVALID_ARG;
+    int v = 0;
+    if (cudaMemcpy(&v, h->scratch + 1, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return NRLDPC_ERR_CUDA;
+    if (v) cudaMemset(h->scratch + 1, 0, sizeof(int));
+    return v ? NRLDPC_ERR_TIMEOUT : NRLDPC_OK;
+}
+
+const char* nrldpc_status_string(int status) {
+    switch (status) {
+        case NRLDPC_OK: return "ok";
+        case NRLDPC_ERR_INVALID_ARG: return "invalid argument";
+        case NRLDPC_ERR_BAD_CONFIG: return "unsupported code configuration";
+        case NRLDPC_ERR_CUDA: return "CUDA error";
+        case NRLDPC_ERR_ALIGNMENT: return "device LLR pointer not 16-byte aligned";
+        case NRLDPC_ERR_TOO_LARGE: return "batch larger than max_batch";
+        case NRLDPC_ERR_TIMEOUT: return "device-side wait timed out";
+        case NRLDPC_ERR_NO_MEMORY: return "allocation failed";
+        case NRLDPC_ERR_NO_DEVICE: return "no usable CUDA device";
+        default: return "unknown status";
+    }
+}
+
+}  // extern "C"

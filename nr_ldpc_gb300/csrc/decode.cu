@@ -1,0 +1,389 @@
+// Fused flooding normalized min-sum decoder for sm_103a.
+//
+// One CTA holds `cpb` whole codewords on chip for all iterations:
+//   * two fp32 posterior buffers per codeword in shared memory, Lold (read by
+//     the check-node pass) and Lnew (accumulates the posterior update);
+//   * the check-node state between iterations, compressed to 16 B per lifted
+//     row (min1, min2, argmin, R sign bits), in a per-CTA slot of global
+//     memory that stays L2-resident (each CTA reuses its slot for every
+//     codeword it takes), streamed with 128-bit loads one row ahead.
+// The LLR batch comes into shared memory with one cp.async.bulk copy per
+// codeword group (mbarrier completion, bounded wait).
+//
+// Bit-exactness with the reference (ctarver/NR_GPU_LDPC):
+//   * check-node arithmetic of src/ldpc_kernels.cu:73-181 (first iteration)
+//     and :199-314: Q = L - R_old, two-min with strict '<' from 1000.0f,
+//     first argmin, R = +-fl(alpha * min) (the reference's
+//     0.75f*sign*sq*min is exact up to the final product), dt = R - R_old;
+//   * variable-node update of src/ldpc_kernels.cu:330-395, 411-468:
+//     APP = L + dt_row0 + dt_row1 + ... in ascending base-row order.  Here
+//     each base row adds its dt into Lnew right after its check-node pass;
+//     rows run in ascending order and a column receives at most one edge per
+//     base row, so every column sees the same fp32 add chain.  Rows between
+//     two CTA barriers share no base column, so their adds commute.
+//   * all float ops are explicit round-to-nearest intrinsics (no FMA
+//     contraction), matching the reference's C semantics.
+//   * hard decision APP > 0 ? 0 : 1, packed LSB-first (src/ldpc_kernels.cu:463-500).
+#include <cuda_runtime.h>
+
+#include "nrldpc_internal.h"
+
+namespace nrldpc {
+namespace {
+
+constexpr int kMaxCpb = 48;
+constexpr int kHeaderBytes = 1024;  // mbarrier, group id, per-slot flags
+constexpr long kWaitLimit = 1L << 20;
+
+__device__ __forceinline__ float max_nan(float a, float b) {
+    float r;
+    asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: false when the limit ran out (the caller records an error).
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+    for (long i = 0; i < kWaitLimit; i++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes,
+                                         uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(dst),
+        "l"(src), "r"(bytes), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// One lifted row (base row with D edges, sub-row s) of one iteration.
+// The first iteration passes a zero state (and a zero previous weight), so
+// R_old = +0 and Q = L - (+0) = L, dt = R - (+0) = R exactly, as in
+// cnp_kernel_1st_iter.  CHECK also accumulates the parity of the hard
+// decisions read from Lold (syndrome of the previous iteration).
+template <int D, bool WEIGHTED, bool CHECK>
+__device__ __forceinline__ void row_update(const CodeTable& tab, int e0, uint32_t s,
+                                           const float* __restrict__ lold, float* lnew,
+                                           const float2* wpair, uint4 st, uint4* st_out,
+                                           float alpha, uint32_t& syn) {
+    const uint32_t z = static_cast<uint32_t>(tab.z);
+    uint32_t addr[D];
+    float lv[D];
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+        const uint32_t ed = tab.edge[e0 + i];
+        uint32_t a = s + (ed & 0xffffu);
+        if (s >= (ed >> 16)) a -= z;  // (s + V) mod Z
+        addr[i] = a;
+        lv[i] = lold[a];
+    }
+    // old messages R_old from the previous iteration's state
+    float rold[D];
+    const float om1 = __uint_as_float(st.x), om2 = __uint_as_float(st.y);
+    const uint32_t oinfo = st.z;
+    const int oidx = static_cast<int>(oinfo & 31u);
+    float oa1 = 0.0f, oa2 = 0.0f;
+    if (!WEIGHTED) {
+        oa1 = __fmul_rn(alpha, om1);
+        oa2 = __fmul_rn(alpha, om2);
+    }
+    float m1 = 1000.0f, m2 = 1000.0f;
+    int idx = 0;
+    uint32_t qmask = 0;
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+        float mag;
+        if (WEIGHTED)
+            mag = __fmul_rn(wpair[e0 + i].x, i == oidx ? om2 : om1);
+        else
+            mag = i == oidx ? oa2 : oa1;
+        const float ro = __uint_as_float(__float_as_uint(mag) | ((oinfo << (23 - i)) & 0x80000000u));
+        rold[i] = ro;
+        const float q = __fsub_rn(lv[i], ro);
+        if (CHECK) syn ^= (lv[i] > 0.0f) ? 0u : 1u;  // hard decision of the posterior read
+        const float qa = fabsf(q);
+        if (q < 0.0f) qmask |= 1u << i;
+        if (qa < m1) idx = i;
+        const float mx = max_nan(m1, qa);  // NaN |Q| leaves min1/min2 untouched
+        m1 = fminf(m1, qa);
+        m2 = fminf(m2, mx);
+    }
+    const uint32_t par = static_cast<uint32_t>(__popc(qmask) & 1);
+    const uint32_t rsign = qmask ^ (0u - par);  // sign of R_i = product of the other signs
+    float a1 = 0.0f, a2 = 0.0f;
+    if (!WEIGHTED) {
+        a1 = __fmul_rn(alpha, m1);
+        a2 = __fmul_rn(alpha, m2);
+    }
+    float nv[D];
+#pragma unroll
+    for (int i = 0; i < D; i++) nv[i] = lnew[addr[i]];
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+        float mag;
+        if (WEIGHTED)
+            mag = __fmul_rn(wpair[e0 + i].y, i == idx ? m2 : m1);
+        else
+            mag = i == idx ? a2 : a1;
+        const float rn = __uint_as_float(__float_as_uint(mag) | ((rsign << (31 - i)) & 0x80000000u));
+        const float dt = __fsub_rn(rn, rold[i]);
+        lnew[addr[i]] = __fadd_rn(nv[i], dt);
+    }
+    if (st_out) {
+        const uint32_t info = static_cast<uint32_t>(idx) | ((rsign & ((1u << D) - 1u)) << 8);
+        __stcg(st_out, make_uint4(__float_as_uint(m1), __float_as_uint(m2), info, 0u));
+    }
+}
+
+template <bool WEIGHTED, bool CHECK>
+__device__ __forceinline__ void row_dispatch(int deg, const CodeTable& tab, int e0, uint32_t s,
+                                             const float* lold, float* lnew, const float2* wpair,
+                                             uint4 st, uint4* st_out, float alpha, uint32_t& syn) {
+    switch (deg) {
+#define NRLDPC_ROW_CASE(D)                                                                   \
+    case D:                                                                                  \
+        row_update<D, WEIGHTED, CHECK>(tab, e0, s, lold, lnew, wpair, st, st_out, alpha, syn); \
+        break;
+        NRLDPC_ROW_CASE(1) NRLDPC_ROW_CASE(2) NRLDPC_ROW_CASE(3) NRLDPC_ROW_CASE(4)
+        NRLDPC_ROW_CASE(5) NRLDPC_ROW_CASE(6) NRLDPC_ROW_CASE(7) NRLDPC_ROW_CASE(8)
+        NRLDPC_ROW_CASE(9) NRLDPC_ROW_CASE(10) NRLDPC_ROW_CASE(11) NRLDPC_ROW_CASE(12)
+        NRLDPC_ROW_CASE(13) NRLDPC_ROW_CASE(14) NRLDPC_ROW_CASE(15) NRLDPC_ROW_CASE(16)
+        NRLDPC_ROW_CASE(17) NRLDPC_ROW_CASE(18) NRLDPC_ROW_CASE(19)
+#undef NRLDPC_ROW_CASE
+        default:
+            break;
+    }
+}
+
+// Hard decisions (and optionally posterior / iteration count) of one codeword
+// slot, written by the slot's Z threads.
+__device__ __forceinline__ void write_outputs(const CodeTable& tab, const float* L, uint32_t s,
+                                              uint8_t* packed, float* app, int32_t* iters,
+                                              int it) {
+    const int n = tab.n_bp, z = tab.z;
+    for (int b = static_cast<int>(s); b < tab.packed_bytes; b += z) {
+        uint32_t v = 0;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            const int c = 8 * b + i;
+            if (c < n && !(L[c] > 0.0f)) v |= 1u << i;
+        }
+        packed[b] = static_cast<uint8_t>(v);
+    }
+    if (app)
+        for (int c = static_cast<int>(s); c < n; c += z) app[c] = L[c];
+    if (iters && s == 0) *iters = it;
+}
+
+// All base rows of one iteration, ascending; returns the OR of the row
+// parities of the hard decisions read (CHECK only).
+template <bool WEIGHTED, bool CHECK>
+__device__ __forceinline__ uint32_t iterate_rows(const CodeTable& tab, uint32_t s, const float* lold,
+                                                 float* lnew, const float2* wpair, uint4* st_base,
+                                                 bool act, bool first, bool last, float alpha) {
+    const int z = tab.z, rows = tab.rows;
+    uint32_t fail = 0;
+    uint4 st_cur = make_uint4(0u, 0u, 0u, 0u);
+    if (!first && act) st_cur = __ldcg(st_base + s);
+    for (int r = 0; r < rows; r++) {
+        uint4 st_next = make_uint4(0u, 0u, 0u, 0u);
+        if (!first && act && r + 1 < rows) st_next = __ldcg(st_base + (r + 1) * z + s);
+        if (act) {
+            uint32_t syn = 0;
+            row_dispatch<WEIGHTED, CHECK>(tab.row_deg[r], tab, tab.row_ptr[r], s, lold, lnew, wpair,
+                                          st_cur, last ? nullptr : st_base + r * z + s, alpha, syn);
+            fail |= syn;
+        }
+        st_cur = st_next;
+        if (tab.sync_after[r]) __syncthreads();
+    }
+    return fail;
+}
+
+// MINB = CTAs per SM the register budget is sized for: 1 when shared memory
+// admits a single CTA per SM anyway (BG1 Z=384), 2 otherwise.
+template <bool WEIGHTED, int MINB>
+__global__ void __launch_bounds__(kMaxThreads, MINB)
+    decode_kernel(const __grid_constant__ CodeTable tab, const __grid_constant__ DecodeArgs a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const uint32_t bar = smem_addr(smem);
+    int* s_group = reinterpret_cast<int*>(smem + 8);
+    int* s_fail = reinterpret_cast<int*>(smem + 16);
+    float2* wpair = reinterpret_cast<float2*>(smem + kHeaderBytes);
+    const int wbytes = WEIGHTED ? kMaxEdges * 8 : 0;
+    float* bufs = reinterpret_cast<float*>(smem + kHeaderBytes + wbytes);
+
+    const int z = tab.z, n = tab.n_bp, cpb = a.cpb, rows = tab.rows;
+    const int tid = threadIdx.x;
+    const int slot = tid / z;
+    const uint32_t s = static_cast<uint32_t>(tid - slot * z);
+    const bool valid_thread = slot < cpb;
+    float* buf0 = bufs;
+    float* buf1 = bufs + static_cast<size_t>(cpb) * n;
+    uint4* st_base =
+        a.state + (static_cast<size_t>(blockIdx.x) * cpb + (valid_thread ? slot : 0)) * rows * z;
+
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+
+    for (;;) {
+        if (tid == 0) *s_group = atomicAdd(a.work_counter, 1);
+        __syncthreads();
+        const int g = *s_group;
+        if (g >= a.n_groups) break;
+        const int cw0 = g * cpb;
+        const int n_valid = min(cpb, a.n_cw - cw0);
+        if (tid == 0) {
+            fence_proxy_async();
+            const uint32_t bytes = static_cast<uint32_t>(n_valid) * n * 4u;
+            mbar_arrive_expect_tx(bar, bytes);
+            bulk_g2s(smem_addr(buf0), a.llr + static_cast<size_t>(cw0) * n, bytes, bar);
+        }
+        bool ok = mbar_wait_bounded(bar, phase);
+        if (!__syncthreads_and(ok)) {
+            if (tid == 0) atomicExch(a.error_flag, kErrLlrLoadTimeout);
+            mbar_wait_bounded(bar, phase);  // let the copy in flight land before leaving
+            return;
+        }
+        phase ^= 1u;
+
+        bool slot_done = !valid_thread || slot >= n_valid;
+        const int cw = cw0 + slot;
+        float* lold = buf0 + static_cast<size_t>(slot) * n;  // per-slot views
+        float* lnew = buf1 + static_cast<size_t>(slot) * n;
+        for (int t = 0; t < a.n_iter; t++) {
+            const bool first = t == 0, last = t == a.n_iter - 1;
+            if (WEIGHTED) {
+                const int nw = a.n_w_iters;
+                const int tp = min(max(t - 1, 0), nw - 1), tc = min(t, nw - 1);
+                for (int e = tid; e < tab.n_edges; e += blockDim.x)  // no previous R at t = 0
+                    wpair[e] = make_float2(first ? 0.0f : a.weights[tp * tab.n_edges + e],
+                                           a.weights[tc * tab.n_edges + e]);
+            }
+            if (tid < cpb) s_fail[tid] = 0;
+            if (!slot_done) {  // Lnew starts as Lold
+                const float4* src = reinterpret_cast<const float4*>(lold);
+                float4* dst = reinterpret_cast<float4*>(lnew);
+                for (int k = static_cast<int>(s); k < n / 4; k += z) dst[k] = src[k];
+            }
+            __syncthreads();
+            const bool act = !slot_done;
+            const bool check = a.early_stop && t > 0;
+            const uint32_t fail =
+                check ? iterate_rows<WEIGHTED, true>(tab, s, lold, lnew, wpair, st_base, act, first,
+                                                    last, a.alpha)
+                      : iterate_rows<WEIGHTED, false>(tab, s, lold, lnew, wpair, st_base, act,
+                                                     first, last, a.alpha);
+            if (check) {
+                if (act && fail) atomicOr(&s_fail[slot], 1);
+                __syncthreads();
+                const bool conv = act && s_fail[slot] == 0;
+                if (conv && cw < a.n_cw) {  // HD of the previous iteration is a codeword
+                    write_outputs(tab, lold, s, a.packed + static_cast<size_t>(cw) * tab.packed_bytes,
+                                  a.app ? a.app + static_cast<size_t>(cw) * n : nullptr,
+                                  a.iters ? a.iters + cw : nullptr, t);
+                }
+                slot_done = slot_done || conv;
+                if (__syncthreads_and(slot_done)) break;
+            }
+            float* tmp = lold;  // the posterior just accumulated is next iteration's input
+            lold = lnew;
+            lnew = tmp;
+            if (last && !slot_done) {
+                write_outputs(tab, lold, s, a.packed + static_cast<size_t>(cw) * tab.packed_bytes,
+                              a.app ? a.app + static_cast<size_t>(cw) * n : nullptr,
+                              a.iters ? a.iters + cw : nullptr, a.n_iter);
+            }
+        }
+        __syncthreads();  // buffers are rewritten by the next group's copy
+    }
+}
+
+}  // namespace
+
+size_t decode_smem_bytes(const CodeTable& tab, int cpb) {
+    return kHeaderBytes + static_cast<size_t>(kMaxEdges) * 8 +
+           2 * static_cast<size_t>(cpb) * tab.n_bp * sizeof(float);
+}
+
+template <bool W, int MINB>
+const void* kernel_ptr() {
+    return reinterpret_cast<const void*>(&decode_kernel<W, MINB>);
+}
+
+const void* select_kernel(bool weighted, int minb) {
+    if (weighted) return minb >= 2 ? kernel_ptr<true, 2>() : kernel_ptr<true, 1>();
+    return minb >= 2 ? kernel_ptr<false, 2>() : kernel_ptr<false, 1>();
+}
+
+cudaError_t decode_kernel_attributes(size_t smem) {
+    for (int w = 0; w < 2; w++)
+        for (int m = 1; m <= 2; m++) {
+            cudaError_t e = cudaFuncSetAttribute(select_kernel(w != 0, m),
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 static_cast<int>(smem));
+            if (e != cudaSuccess) return e;
+        }
+    return cudaSuccess;
+}
+
+int decode_max_ctas_per_sm(bool weighted, int minb, int threads, size_t smem) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, select_kernel(weighted, minb), threads,
+                                                      smem) != cudaSuccess)
+        return 0;
+    return n;
+}
+
+cudaError_t launch_decode(const CodeTable& tab, const DecodeArgs& args, int grid, int threads,
+                          size_t smem, bool weighted, int minb, cudaStream_t stream) {
+    if (args.cpb < 1 || args.cpb > kMaxCpb) return cudaErrorInvalidValue;
+    if (weighted) {
+        if (minb >= 2)
+            decode_kernel<true, 2><<<grid, threads, smem, stream>>>(tab, args);
+        else
+            decode_kernel<true, 1><<<grid, threads, smem, stream>>>(tab, args);
+    } else {
+        if (minb >= 2)
+            decode_kernel<false, 2><<<grid, threads, smem, stream>>>(tab, args);
+        else
+            decode_kernel<false, 1><<<grid, threads, smem, stream>>>(tab, args);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace nrldpc

@@ -1,0 +1,73 @@
+// Internal types shared by the CUDA sources and the C-ABI layer.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace nrldpc {
+
+constexpr int kMaxRows = 46;    // BG1
+constexpr int kMaxCols = 68;    // BG1
+constexpr int kMaxEdges = 320;  // BG1 has 316
+constexpr int kMaxDeg = 19;     // BG1 rows 0..3
+constexpr int kMaxZ = 384;
+constexpr int kMaxThreads = 384;  // decode CTA size bound (cw_per_cta * Z)
+
+// Lifted-code description passed to kernels by value (__grid_constant__).
+struct CodeTable {
+    int rows, cols, z, n_edges, n_bp, packed_bytes;
+    int kb;                        // systematic base columns (encoder)
+    uint16_t row_ptr[kMaxRows + 1];
+    uint8_t row_deg[kMaxRows];
+    uint8_t sync_after[kMaxRows];  // 1: CTA barrier after this row (row groups
+                                   // between barriers share no base column)
+    // per edge, row-major ascending (row, then column) = the reference's
+    // h_compact1 order: low 16 bits blk_col*Z + V, high 16 bits Z - V
+    uint32_t edge[kMaxEdges];
+    uint8_t edge_col[kMaxEdges];
+    uint16_t edge_shift[kMaxEdges];  // V mod Z
+};
+
+// Check-node state of one lifted row, kept between iterations (16 B):
+//   x = min1 (raw |Q|), y = min2, z = idx (bits 0..4) | R sign of edge i at
+//   bit 8+i, w = unused.
+struct DecodeArgs {
+    const float* llr;
+    uint8_t* packed;
+    float* app;
+    int32_t* iters;
+    uint4* state;           // [grid * cpb][rows * Z]
+    int* work_counter;      // dynamic codeword-group scheduler, zeroed per launch
+    int* error_flag;        // bounded-wait failures
+    const float* weights;   // [n_w_iters][n_edges] or null
+    int n_cw, n_iter, cpb, n_groups, n_w_iters, early_stop;
+    float alpha;
+};
+
+enum DeviceError : int { kErrNone = 0, kErrLlrLoadTimeout = 1 };
+
+// Host-side launchers (decode.cu / channel.cu).
+// minb: CTAs per SM the kernel's register budget assumes (1 or 2).
+cudaError_t launch_decode(const CodeTable& tab, const DecodeArgs& args, int grid, int threads,
+                          size_t smem, bool weighted, int minb, cudaStream_t stream);
+size_t decode_smem_bytes(const CodeTable& tab, int cpb);
+cudaError_t decode_kernel_attributes(size_t smem);
+int decode_max_ctas_per_sm(bool weighted, int minb, int threads, size_t smem);
+
+struct EncodePlan {
+    int n_core_steps;              // rows solved one parity column at a time
+    int core_row[kMaxRows];
+    int core_col[kMaxRows];
+    int p0_col, p0_shift;          // first parity column = P^{-v} * sum(lambda)
+    int n_stair;                   // staircase rows summed for p0
+};
+bool make_encode_plan(const CodeTable& tab, EncodePlan* plan);
+cudaError_t launch_gen_llr(const CodeTable& tab, const EncodePlan& plan, uint64_t seed,
+                           uint64_t cw_base, int n_cw, const float* sigma, int n_punct_cols,
+                           float* llr, uint8_t* cw_packed, cudaStream_t stream);
+cudaError_t launch_count_errors(const uint8_t* packed, const uint8_t* cw_packed, int n_cw,
+                                int packed_bytes, int n_info, unsigned long long* counts,
+                                cudaStream_t stream);
+
+}  // namespace nrldpc

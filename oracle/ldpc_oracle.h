@@ -1,0 +1,96 @@
+/*
+ * CPU oracle for the QC-LDPC min-sum decode path -- TEST INFRASTRUCTURE ONLY.
+ *
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may
+ * load this library, and only as the checker (or the timed CPU baseline).
+ * The decoder product never links or calls it.
+ *
+ * What it restates (reference = ctarver/NR_GPU_LDPC):
+ *   - compact row/column edge orders: src/setup_exp.cu:221-271
+ *   - first-iteration check-node pass:  src/ldpc_kernels.cu:73-181
+ *   - check-node pass, iterations >= 2: src/ldpc_kernels.cu:199-314
+ *   - variable-node pass (incremental posterior, ascending base rows):
+ *                                       src/ldpc_kernels.cu:330-395, 411-468
+ *   - hard-decision packing (LSB first): src/ldpc_kernels.cu:482-500
+ *   - iteration orchestration:          src/gpu_decoder_top.cu:25-49
+ * Float semantics are the reference's float branch on a signed-char
+ * platform with every C statement rounded on its own (built with
+ * -ffp-contract=off).  Pinned against the reference's own kernel source run
+ * on the CPU (oracle/_ref) through the committed fixtures in tests/golden.
+ *
+ * Additions with no reference counterpart (their own oracles): syndrome early
+ * stop, FP64 twin, learned weighted min-sum forward/adjoint, a structural
+ * encoder, and a Philox4x32-10 + Box-Muller channel generator whose float
+ * arithmetic is written so the GPU generator reproduces it bit for bit.
+ */
+#ifndef NR_LDPC_ORACLE_H
+#define NR_LDPC_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_code orc_code;
+
+/* Build a lifted code from a dense base matrix (rows x cols, -1 = zero block,
+ * otherwise the table shift V; V is reduced mod Z).  Returns NULL on error. */
+orc_code* orc_code_new(const int* base, int rows, int cols, int z);
+void orc_code_free(orc_code* c);
+int orc_code_edges(const orc_code* c);
+
+/* Flooding normalized min-sum, fp32, reference semantics.
+ *   llr     [n_cw][cols*Z]         channel LLRs (punctured columns = 0)
+ *   packed  [n_cw][ceil(cols*Z/8)]       hard decisions, bit i of byte b = bit 8b+i
+ *   app     [n_cw][cols*Z] or NULL final posterior (APP of the last iteration)
+ *   iters   [n_cw] or NULL         iterations after which HD was taken
+ * early_stop != 0: stop after iteration t when the syndrome of HD_t is zero.
+ * n_threads > 1 decodes codewords on that many POSIX threads. */
+int orc_minsum_f32(const orc_code* c, const float* llr, int n_cw, int n_iter, float alpha,
+                   int early_stop, uint8_t* packed, float* app, int32_t* iters, int n_threads);
+
+/* The same algorithm carried out in double precision (alpha exact). */
+int orc_minsum_f64(const orc_code* c, const double* llr, int n_cw, int n_iter, double alpha,
+                   int early_stop, uint8_t* packed, double* app, int32_t* iters);
+
+/* Syndrome weight (number of unsatisfied lifted checks) of packed bits. */
+int orc_syndrome_weight(const orc_code* c, const uint8_t* packed);
+
+/* Structural encoder.  kb systematic base columns, info = kb*Z bits (one per
+ * byte, 0/1), cw_packed = ceil(cols*Z/8) bytes.  Returns 0 or a negative error. */
+int orc_encode(const orc_code* c, int kb, const uint8_t* info, uint8_t* cw_packed);
+
+/* Channel generator: for codeword id (cw_base + i), draw kb*Z info bits,
+ * encode, BPSK (0 -> +1), add Gaussian noise sigma[i], LLR = (2y)/(sigma^2);
+ * the first n_punct columns' LLRs are 0 (punctured), as are LLRs of columns
+ * beyond n_tx transmitted bits.  Outputs: llr [n_cw][cols*Z],
+ * cw_packed [n_cw][ceil(cols*Z/8)] (may be NULL). */
+int orc_gen_llr(const orc_code* c, int kb, uint64_t seed, uint64_t cw_base, int n_cw,
+                const float* sigma, int n_punct_cols, float* llr, uint8_t* cw_packed);
+
+/* Philox4x32-10 block (Salmon et al., SC'11) and the float helpers used by the
+ * generator, exposed for the generator's own tests. */
+void orc_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+float orc_logf(float x);
+void orc_sincos2pi(float u, float* s, float* c);
+
+/* ---- learned weighted min-sum (per iteration t, per base edge e weights) ----
+ * Forward (double): R^t_e = w[t][e] * sign * min (extrinsic), posterior
+ * L^{t+1} = llr + sum_e R^t_e, loss = mean over t=1..T, codewords and columns
+ * of softplus(-y*L^t), y = +1 for bit 0 and -1 for bit 1.
+ * grad (may be NULL) receives dloss/dw [T][edges] by the adjoint recursion.
+ * app (may be NULL) receives L^T. Returns the loss. */
+double orc_wms_loss_grad_f64(const orc_code* c, const float* llr, const uint8_t* cw_packed,
+                             int n_cw, int n_iter, const double* w, double* grad, double* app);
+
+/* fp32 forward of the weighted decoder as an inference decoder (weights
+ * replace alpha; t >= n_weight_iters reuse the last row).  Same outputs as
+ * orc_minsum_f32. */
+int orc_wms_decode_f32(const orc_code* c, const float* llr, int n_cw, int n_iter,
+                       const float* w, int n_weight_iters, int early_stop, uint8_t* packed,
+                       float* app, int32_t* iters);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,229 @@
+"""ctypes binding of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Imported by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg,
+and nowhere else.  ``RefEmu`` loads oracle/_ref (the reference's own kernel
+source run on the CPU), which exists only where the reference tree was
+present at build time.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_lib = None
+
+
+def build(reference_root: str | None = None, quiet: bool = True) -> None:
+    """Run oracle/Makefile (the oracle, plus oracle/_ref if the reference exists)."""
+    cmd = ["make", "-C", HERE]
+    if reference_root:
+        cmd.append(f"REF={reference_root}")
+    subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL if quiet else None)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            subprocess.run(["make", "-C", HERE, os.path.join("_build", "liboracle.so")],
+                           check=True, stdout=subprocess.DEVNULL)
+        L = C.CDLL(LIB_PATH)
+        L.orc_code_new.restype = C.c_void_p
+        L.orc_code_new.argtypes = [_i32p, C.c_int, C.c_int, C.c_int]
+        L.orc_code_free.argtypes = [C.c_void_p]
+        L.orc_code_edges.argtypes = [C.c_void_p]
+        L.orc_minsum_f32.argtypes = [C.c_void_p, _f32p, C.c_int, C.c_int, C.c_float, C.c_int,
+                                     _u8p, C.c_void_p, C.c_void_p, C.c_int]
+        L.orc_minsum_f64.argtypes = [C.c_void_p, _f64p, C.c_int, C.c_int, C.c_double, C.c_int,
+                                     _u8p, C.c_void_p, C.c_void_p]
+        L.orc_syndrome_weight.argtypes = [C.c_void_p, _u8p]
+        L.orc_encode.argtypes = [C.c_void_p, C.c_int, _u8p, _u8p]
+        L.orc_gen_llr.argtypes = [C.c_void_p, C.c_int, C.c_uint64, C.c_uint64, C.c_int, _f32p,
+                                  C.c_int, _f32p, C.c_void_p]
+        L.orc_philox4x32.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                     C.POINTER(C.c_uint32)]
+        L.orc_logf.restype = C.c_float
+        L.orc_logf.argtypes = [C.c_float]
+        L.orc_sincos2pi.argtypes = [C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+        L.orc_wms_loss_grad_f64.restype = C.c_double
+        L.orc_wms_loss_grad_f64.argtypes = [C.c_void_p, _f32p, _u8p, C.c_int, C.c_int, _f64p,
+                                            C.c_void_p, C.c_void_p]
+        L.orc_wms_decode_f32.argtypes = [C.c_void_p, _f32p, C.c_int, C.c_int, _f32p, C.c_int,
+                                         C.c_int, _u8p, C.c_void_p, C.c_void_p]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class OracleCode:
+    """A lifted code in the oracle: base matrix (V, -1 empty) and Z."""
+
+    def __init__(self, base: np.ndarray, z: int):
+        base = np.ascontiguousarray(base, dtype=np.int32)
+        self.rows, self.cols = base.shape
+        self.z = int(z)
+        self.n_bp = self.cols * self.z
+        self.n_bytes = (self.n_bp + 7) // 8
+        self.base = base
+        self._h = lib().orc_code_new(base, self.rows, self.cols, self.z)
+        if not self._h:
+            raise ValueError("bad base matrix")
+        self.n_edges = lib().orc_code_edges(self._h)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.orc_code_free(self._h)
+            self._h = None
+
+    def minsum_f32(self, llr, n_iter, alpha=0.75, early_stop=False, want_app=False, threads=1):
+        llr = np.ascontiguousarray(llr, dtype=np.float32).reshape(-1, self.n_bp)
+        n = llr.shape[0]
+        packed = np.zeros((n, self.n_bytes), np.uint8)
+        app = np.zeros((n, self.n_bp), np.float32) if want_app else None
+        iters = np.zeros(n, np.int32)
+        rc = lib().orc_minsum_f32(self._h, llr, n, int(n_iter), float(alpha), int(early_stop),
+                                  packed, _ptr(app), _ptr(iters), int(threads))
+        if rc:
+            raise RuntimeError(f"orc_minsum_f32 rc={rc}")
+        return packed, app, iters
+
+    def minsum_f64(self, llr, n_iter, alpha=0.75, early_stop=False):
+        llr = np.ascontiguousarray(llr, dtype=np.float64).reshape(-1, self.n_bp)
+        n = llr.shape[0]
+        packed = np.zeros((n, self.n_bytes), np.uint8)
+        app = np.zeros((n, self.n_bp), np.float64)
+        iters = np.zeros(n, np.int32)
+        rc = lib().orc_minsum_f64(self._h, llr, n, int(n_iter), float(alpha), int(early_stop),
+                                  packed, _ptr(app), _ptr(iters))
+        if rc:
+            raise RuntimeError(f"orc_minsum_f64 rc={rc}")
+        return packed, app, iters
+
+    def syndrome_weight(self, packed_cw) -> int:
+        return lib().orc_syndrome_weight(self._h, np.ascontiguousarray(packed_cw, np.uint8))
+
+    def encode(self, kb, info_bits):
+        out = np.zeros(self.n_bytes, np.uint8)
+        rc = lib().orc_encode(self._h, int(kb), np.ascontiguousarray(info_bits, np.uint8), out)
+        if rc:
+            raise RuntimeError(f"orc_encode rc={rc}")
+        return out
+
+    def gen_llr(self, kb, seed, cw_base, sigma, n_punct_cols):
+        sigma = np.ascontiguousarray(np.atleast_1d(sigma), np.float32)
+        n = sigma.shape[0]
+        llr = np.zeros((n, self.n_bp), np.float32)
+        cw = np.zeros((n, self.n_bytes), np.uint8)
+        rc = lib().orc_gen_llr(self._h, int(kb), int(seed), int(cw_base), n, sigma,
+                               int(n_punct_cols), llr, _ptr(cw))
+        if rc:
+            raise RuntimeError(f"orc_gen_llr rc={rc}")
+        return llr, cw
+
+    def wms_loss_grad(self, llr, cw_packed, n_iter, w, want_grad=True):
+        llr = np.ascontiguousarray(llr, np.float32).reshape(-1, self.n_bp)
+        n = llr.shape[0]
+        w = np.ascontiguousarray(w, np.float64).reshape(n_iter, self.n_edges)
+        grad = np.zeros_like(w) if want_grad else None
+        app = np.zeros((n, self.n_bp), np.float64)
+        loss = lib().orc_wms_loss_grad_f64(self._h, llr, np.ascontiguousarray(cw_packed, np.uint8),
+                                           n, int(n_iter), w, _ptr(grad), _ptr(app))
+        return loss, grad, app
+
+    def wms_decode_f32(self, llr, n_iter, w, early_stop=False, want_app=False):
+        llr = np.ascontiguousarray(llr, dtype=np.float32).reshape(-1, self.n_bp)
+        w = np.ascontiguousarray(w, np.float32).reshape(-1, self.n_edges)
+        n = llr.shape[0]
+        packed = np.zeros((n, self.n_bytes), np.uint8)
+        app = np.zeros((n, self.n_bp), np.float32) if want_app else None
+        iters = np.zeros(n, np.int32)
+        rc = lib().orc_wms_decode_f32(self._h, llr, n, int(n_iter), w, w.shape[0],
+                                      int(early_stop), packed, _ptr(app), _ptr(iters))
+        if rc:
+            raise RuntimeError(f"orc_wms_decode_f32 rc={rc}")
+        return packed, app, iters
+
+
+def philox4x32(ctr, key):
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    lib().orc_philox4x32(c, k, o)
+    return list(o)
+
+
+class RefEmu:
+    """The reference's own decoder source run on the CPU (oracle/_ref)."""
+
+    KIND = {(46, 68): "bg1", (42, 52): "bg2", (12, 24): "wifi"}
+
+    def __init__(self, base: np.ndarray, z: int):
+        kind = self.KIND[tuple(base.shape)]
+        path = os.path.join(REF_DIR, f"libref_{kind}.so")
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        self.L = C.CDLL(path)
+        self.L.ref_init_code.argtypes = [_i32p, C.c_int, C.c_int, C.c_int]
+        self.L.ref_decode.argtypes = [_f32p, C.c_int, C.c_int, _u8p, C.c_void_p]
+        self.L.ref_setup_ldpc.argtypes = [C.c_int, C.c_float, C.c_int, _i32p]
+        self.L.ref_transmit_llr.argtypes = [C.c_int, C.c_float, C.c_int, C.c_float, C.c_uint,
+                                            _f32p, _i32p]
+        h = np.ascontiguousarray(base, np.int32).copy()
+        h[h >= 0] %= int(z)
+        self.rows, self.cols = h.shape
+        self.z = int(z)
+        self.n_bp = self.cols * self.z
+        self.n_bytes = (self.n_bp + 7) // 8
+        rc = self.L.ref_init_code(h, self.rows, self.cols, self.z)
+        if rc:
+            raise RuntimeError(f"ref_init_code rc={rc}")
+
+    @staticmethod
+    def available(kind="bg1") -> bool:
+        return os.path.exists(os.path.join(REF_DIR, f"libref_{kind}.so"))
+
+    def decode(self, llr, n_iter, want_app=False, chunk=16):
+        llr = np.ascontiguousarray(llr, dtype=np.float32).reshape(-1, self.n_bp)
+        n = llr.shape[0]
+        packed = np.zeros((n, self.n_bytes), np.uint8)
+        app = np.zeros((n, self.n_bp), np.float32) if want_app else None
+        for s in range(0, n, chunk):
+            e = min(n, s + chunk)
+            pk = np.zeros((e - s, self.n_bytes), np.uint8)
+            ap = np.zeros((e - s, self.n_bp), np.float32) if want_app else None
+            rc = self.L.ref_decode(np.ascontiguousarray(llr[s:e]), e - s, int(n_iter), pk, _ptr(ap))
+            if rc:
+                raise RuntimeError(f"ref_decode rc={rc}")
+            packed[s:e] = pk
+            if want_app:
+                app[s:e] = ap
+        return packed, app
+
+    def setup_ldpc(self, A, rate, n_iter):
+        out = np.zeros(12, np.int32)
+        self.L.ref_setup_ldpc(int(A), float(rate), int(n_iter), out)
+        keys = ["A", "bg_index", "Z", "K", "N", "H_rows", "H_cols", "n_nz_in_row", "n_nz_in_col",
+                "n_iterations", "N_before_puncture", "H00"]
+        return dict(zip(keys, out.tolist()))
+
+    def transmit_llr(self, A, rate, n_cw, ebn0_db, seed, K, n_bp):
+        llr = np.zeros((n_cw, n_bp), np.float32)
+        info = np.zeros((n_cw, K), np.int32)
+        rc = self.L.ref_transmit_llr(int(A), float(rate), int(n_cw), float(ebn0_db), int(seed), llr, info)
+        if rc:
+            raise RuntimeError(f"ref_transmit_llr rc={rc}")
+        return llr, info
