@@ -1,0 +1,320 @@
+"""Benchmark: 5G NR BG1 Z=384 normalized min-sum decode throughput on GB300.
+
+One step = one decode of a batch of 4096 BG1 Z=384 codewords (K=8448 info
+bits, N_bp=26112 fp32 LLRs each, 428 MB per batch -- larger than L2), 10
+flooding iterations, early stop off, at an Eb/N0 where the batch's FER is
+<= 1e-2.  ``value`` is info Gbit/s with the LLRs resident in HBM; ``e2e`` is
+the same metric through the reference-shaped host call
+(nrldpc_decode_host_async: pinned host LLRs -> device -> packed bits back).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun each rank decodes its own batch (codewords are independent:
+replicas, weak scaling); rank 0 prints one JSON line with the max time over
+ranks.  ``--impl reference`` times the reference algorithm's CPU
+implementation (the C restatement in oracle/, all host cores).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "info Gbit/s at FER<=1e-2 (BG1 Z=384 normalized min-sum, 10 iterations)"
+BG, Z, ITERS, BATCH, EBN0 = 1, 384, 10, 4096, 2.0
+K_INFO, N_BP, E_EDGES = 8448, 26112, 316
+
+
+def model_bytes_per_cw(n_iter: int) -> int:
+    """Algorithmic bytes of one codeword: LLR in + packed HD out + per
+    iteration one fp32 read and write of every lifted edge message and of
+    every posterior: 4*N_bp + N_bp/8 + I*8*(E*Z + N_bp)."""
+    return 4 * N_BP + N_BP // 8 + n_iter * 8 * (E_EDGES * Z + N_BP)
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_cw():
+    """DRAM bytes per codeword of the decode kernel from the committed ncu
+    summary (dram__bytes_read.sum + dram__bytes_write.sum of one launch,
+    divided by the codewords that launch decoded)."""
+    p = os.path.join(ROOT, "profiles", "decode_bg1_z384_dram.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    return float(d["dram_bytes_per_cw"])
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        pw = [float(r[3]) for r in rows if r[3].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        pmax = max(pw) if pw else 0.0
+        loaded = [s for s, p in zip(sm, pw) if p >= 0.5 * pmax] if sm and pw else sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "power_w_max": max(pw) if pw else None, "samples": len(rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_e2e(dec, llr, packed, steps, stream, world):
+    """Same decode through the host-buffer C-ABI call: pinned host LLRs ->
+    H2D -> decode -> D2H of packed bits, each step synchronized."""
+    import torch
+    b = llr.shape[0]
+    llr_h = torch.empty((b, N_BP), dtype=torch.float32, pin_memory=True)
+    llr_h.copy_(llr)
+    out_h = torch.empty((b, dec.packed_bytes), dtype=torch.uint8, pin_memory=True)
+    for _ in range(2):
+        dec.decode_host(llr_h, out_h, ITERS, stream=stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        dec.decode_host(llr_h, out_h, ITERS, stream=stream)
+        stream.synchronize()
+    e2e_ms = 1e3 * (time.perf_counter() - t0) / steps
+    e2e_ms = max_over_ranks(e2e_ms, world)
+    assert torch.equal(out_h, packed.cpu()), "host-path output differs from device path"
+    return e2e_ms
+
+
+def cpu_baseline(llr_host: np.ndarray, n_sample: int):
+    """Reference algorithm on the host cores: the oracle's C restatement of
+    the reference min-sum (kind 'port'), all cores, one codeword per thread."""
+    from nr_ldpc_gb300 import codes
+    from oracle.oracle import OracleCode
+    oc = OracleCode(codes.base_matrix(BG, codes.set_index(Z)), Z)
+    cores = os.cpu_count() or 1
+    sample = np.ascontiguousarray(llr_host[:n_sample])
+    oc.minsum_f32(sample[:cores], 1, threads=cores)  # warm
+    t0 = time.perf_counter()
+    oc.minsum_f32(sample, ITERS, threads=cores)
+    dt = time.perf_counter() - t0
+    n1 = min(8, n_sample)
+    t0 = time.perf_counter()
+    oc.minsum_f32(sample[:n1], ITERS, threads=1)
+    dt1 = time.perf_counter() - t0
+    return {"value": n_sample * K_INFO / dt / 1e9, "unit": "Gbit/s", "cores": cores, "kind": "port",
+            "sample": f"{n_sample} BG1 Z=384 codewords of the bench batch, {ITERS} iterations, "
+                      f"{cores} threads ({dt:.2f} s)",
+            "value_1thread": n1 * K_INFO / dt1 / 1e9}
+
+
+def run_reference(args, world, rank):
+    """--impl reference: the reference algorithm on the host cores (oracle
+    port; the reference's own decoder exists only as CUDA kernels that do not
+    build for sm_103a / CUDA 13 as shipped)."""
+    if rank != 0:
+        return
+    from nr_ldpc_gb300 import codes
+    from oracle.oracle import OracleCode
+    oc = OracleCode(codes.base_matrix(BG, codes.set_index(Z)), Z)
+    cores = os.cpu_count() or 1
+    n_step = max(cores * 4, 64)
+    sig = np.full(n_step, codes.noise_sigma(EBN0, K_INFO / (N_BP - 2 * Z)), np.float32)
+    llr, _ = oc.gen_llr(22, 2024, 0, sig, 2)
+    for _ in range(args.warmup):
+        oc.minsum_f32(llr[:cores], ITERS, threads=cores)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oc.minsum_f32(llr, ITERS, threads=cores)
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * sum(times) / len(times)
+    value = n_step * K_INFO / (ms * 1e-3) / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Gbit/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded Philox info bits, BPSK/AWGN LLRs)",
+        "config": {"workload": f"BG1 Z=384 min-sum decode, {ITERS} iterations, Eb/N0 {EBN0} dB",
+                   "codewords_per_step": n_step, "threads": cores},
+        "cpu_baseline": {"value": value, "unit": "Gbit/s", "cores": cores, "kind": "port",
+                         "sample": f"{n_step} codewords per step on {cores} threads"},
+        "e2e": {"value": value, "unit": "Gbit/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling)")
+    ap.add_argument("--batch", type=int, default=BATCH,
+                    help="codewords per step (profiling a smaller launch; default 4096)")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_setup()
+    B = args.batch
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from nr_ldpc_gb300 import Decoder, codes
+
+    dec = Decoder(bg=BG, z=Z, max_batch=B, device=local)
+    stream = torch.cuda.current_stream()
+    sigma = codes.noise_sigma(EBN0, K_INFO / (N_BP - 2 * Z))
+    sig = torch.full((B,), sigma, dtype=torch.float32, device="cuda")
+    llr, cw = dec.gen_llr(seed=7, cw_base=rank * B, sigma=sig)
+    packed = torch.empty((B, dec.packed_bytes), dtype=torch.uint8, device="cuda")
+    for _ in range(args.warmup):
+        dec.decode(llr, ITERS, out=packed)
+    torch.cuda.synchronize()
+    counts = dec.count_errors(packed, cw)
+    torch.cuda.synchronize()
+    bit_err, frame_err = counts.tolist()
+
+    # ---- device-resident timed region --------------------------------------------
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    t_all0 = torch.cuda.Event(enable_timing=True)
+    t_all1 = torch.cuda.Event(enable_timing=True)
+    t_all0.record(stream)
+    for i in range(args.steps):
+        ev[i][0].record(stream)
+        dec.decode(llr, ITERS, out=packed, stream=stream)
+        ev[i][1].record(stream)
+    t_all1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = sampler.stop()
+    ms_step = t_all0.elapsed_time(t_all1) / args.steps
+    ms_launch = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+    ms_step = max_over_ranks(ms_step, world)
+    value = world * B * K_INFO / (ms_step * 1e-3) / 1e9
+
+    # ---- end to end through the host-buffer C-ABI call -----------------------------
+    e2e_ms = float("nan")
+    if not args.no_e2e:
+        e2e_ms = run_e2e(dec, llr, packed, args.steps, stream, world)
+
+    peak, peak_kind = measured_peaks()
+    bytes_launch = model_bytes_per_cw(ITERS) * B
+    achieved = bytes_launch / (ms_launch * 1e-3) / 1e9
+    tpc = traffic_per_cw()
+    line = {
+        "metric": METRIC, "value": value, "unit": "Gbit/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded Philox info bits, structural encoder, BPSK/AWGN LLRs)",
+        "config": {"workload": "BG1 Z=384 normalized min-sum (alpha 0.75) flooding decode, "
+                               f"batch {B}, {ITERS} iterations, early stop off",
+                   "ebn0_db": EBN0, "codewords_per_gpu": B, "info_bits": K_INFO,
+                   "fer": frame_err / B, "ber": bit_err / (B * K_INFO),
+                   "l2_policy": f"inputs larger than L2 ({B * N_BP * 4 / 1e6:.0f} MB LLR batch per step)",
+                   "parallelism": f"replicas x{world}"},
+        "cw_per_s": world * B / (ms_step * 1e-3),
+        "e2e": {"value": world * B * K_INFO / (e2e_ms * 1e-3) / 1e9, "unit": "Gbit/s",
+                "h2d_bytes_per_step": B * N_BP * 4, "d2h_bytes_per_step": B * dec.packed_bytes,
+                "ms_per_step": e2e_ms},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": None if tpc is None else tpc * B,
+                     "model_bytes_per_launch": bytes_launch, "kernel_ms": ms_launch},
+        "clocks": clocks,
+        "gpu_launches": args.steps,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(llr.cpu().numpy(), n_sample=min(B, 1024))
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    dec.close()
+
+
+if __name__ == "__main__":
+    main()

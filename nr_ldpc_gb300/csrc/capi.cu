@@ -72,13 +72,13 @@ bool fill_table(const int* base, int rows, int cols, int z, int kb, CodeTable* t
     t->n_edges = e;
     // Barrier placement: greedy groups of consecutive rows that pairwise share
     // no base column; a barrier closes each group.
-    std::vector<int> used(cols, 0);
+    int used[kMaxCols] = {0};
     for (int r = 0; r < rows; r++) {
         bool clash = false;
         for (int k = t->row_ptr[r]; k < t->row_ptr[r + 1]; k++) clash |= used[t->edge_col[k]] != 0;
         if (clash) {
             t->sync_after[r - 1] = 1;
-            std::fill(used.begin(), used.end(), 0);
+            std::fill(used, used + kMaxCols, 0);
         }
         for (int k = t->row_ptr[r]; k < t->row_ptr[r + 1]; k++) used[t->edge_col[k]] = 1;
     }
@@ -211,6 +211,18 @@ int decode_impl(Handle* h, const float* llr, uint8_t* packed, int n_cw, int n_it
 }
 
 }  // namespace
+
+namespace nrldpc {
+// Lifted-code table of 5G NR (bg, z) without any heap allocation.
+bool make_nr_table(int bg, int z, CodeTable* t) {
+    const int ils = nrldpc_set_index(z);
+    if ((bg != 1 && bg != 2) || ils < 0) return false;
+    int H[kMaxRows * kMaxCols];
+    int rows = 0, cols = 0;
+    if (base_matrix_impl(bg, ils, H, &rows, &cols) != NRLDPC_OK) return false;
+    return fill_table(H, rows, cols, z, bg == 1 ? 22 : 10, t);
+}
+}  // namespace nrldpc
 
 extern "C" {
 

@@ -55,6 +55,9 @@ size_t decode_smem_bytes(const CodeTable& tab, int cpb);
 cudaError_t decode_kernel_attributes(size_t smem);
 int decode_max_ctas_per_sm(bool weighted, int minb, int threads, size_t smem);
 
+// 5G NR (bg, z) code table, built on the caller's storage (no allocation).
+bool make_nr_table(int bg, int z, CodeTable* t);
+
 struct EncodePlan {
     int n_core_steps;              // rows solved one parity column at a time
     int core_row[kMaxRows];

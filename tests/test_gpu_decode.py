@@ -1,0 +1,202 @@
+"""GPU decode parity through the C-ABI: golden fixtures made from the
+reference's own kernels, the oracle on seeded and adversarial inputs, and
+size-independent properties at the full 4096-codeword BG1 Z=384 batch."""
+import ctypes as C
+import hashlib
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from nr_ldpc_gb300 import Decoder, _lib, codes
+from oracle.oracle import OracleCode
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def make_decoder(case_or_bg, z=None, max_batch=64, **kw):
+    if isinstance(case_or_bg, dict):
+        case = case_or_bg
+        if case["code"] == "wifi":
+            return Decoder(z=case["z"], base=codes.wifi_base(), max_batch=max_batch, **kw)
+        return Decoder(bg=case["bg"], z=case["z"], max_batch=max_batch, **kw)
+    return Decoder(bg=case_or_bg, z=z, max_batch=max_batch, **kw)
+
+
+def bits_nan_canonical(a: np.ndarray) -> np.ndarray:
+    """fp32 bit patterns with every NaN mapped to one pattern (IEEE 754
+    leaves NaN payloads unspecified: the GPU returns 0x7fffffff, x86 0x7fc00000)."""
+    b = np.ascontiguousarray(a, np.float32).view(np.uint32).copy()
+    b[np.isnan(a)] = 0x7FC00000
+    return b
+
+
+def oracle_for(dec: Decoder):
+    base = codes.wifi_base() if dec.cols == 24 else codes.base_matrix(dec.bg, codes.set_index(dec.z))
+    return OracleCode(base, dec.z)
+
+
+@pytest.mark.parametrize("idx", range(15))
+def test_golden_fixture(golden, gpu, idx):
+    """Hard decisions and posterior bits equal the reference kernels'."""
+    case = golden["cases"][idx]
+    dec = make_decoder(case)
+    oc = oracle_for(dec)
+    sig = np.full(case["n_cw"], case["sigma"], np.float32)
+    llr, cw = oc.gen_llr(case["kb"], case["seed"], case["cw_base"], sig, case["n_punct_cols"])
+    assert sha(llr) == case["llr_sha256"]
+    d_llr = torch.from_numpy(llr).to(gpu)
+    for it, res in case["results"].items():
+        packed, app = dec.decode(d_llr, int(it), want_app=True)
+        torch.cuda.synchronize()
+        assert sha(packed.cpu().numpy()) == res["packed_sha256"], f"{case['name']} I={it}"
+        assert sha(app.cpu().numpy()) == res["app_sha256"], f"{case['name']} I={it} posterior"
+    assert dec.device_error() == 0
+
+
+def test_reference_channel_pipeline_fixture(golden, gpu):
+    """LLRs from the reference's own OAI encoder + drand48 AWGN pipeline."""
+    pipe = golden["ref_pipeline"]
+    llr = np.load(os.path.join(GOLDEN, "ref_pipeline_bg1_z384_llr.npy"))
+    dec = Decoder(bg=1, z=384, max_batch=4)
+    for it, res in pipe["results"].items():
+        packed, app = dec.decode(torch.from_numpy(llr).to(gpu), int(it), want_app=True)
+        torch.cuda.synchronize()
+        assert sha(packed.cpu().numpy()) == res["packed_sha256"]
+        assert sha(app.cpu().numpy()) == res["app_sha256"]
+
+
+@pytest.mark.parametrize("bg,z", [(1, 384), (2, 128), (1, 96), (2, 7), (1, 15), (2, 384), (1, 2)])
+def test_generator_bit_identical_to_oracle(gpu, bg, z):
+    dec = make_decoder(bg, z, max_batch=16)
+    oc = oracle_for(dec)
+    sig = np.linspace(0.6, 1.3, 9).astype(np.float32)
+    llr, cw = oc.gen_llr(dec.kb, 1234567, 99, sig, 2)
+    g_llr, g_cw = dec.gen_llr(1234567, 99, torch.from_numpy(sig).to(gpu), 2)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(g_llr.cpu().numpy().view(np.uint32), llr.view(np.uint32))
+    np.testing.assert_array_equal(g_cw.cpu().numpy(), cw)
+    for i in range(cw.shape[0]):
+        assert oc.syndrome_weight(cw[i]) == 0
+
+
+@pytest.mark.parametrize("bg,z,cpb", [(1, 384, 0), (2, 128, 0), (1, 64, 0), (1, 64, 1), (1, 64, 4),
+                                      (2, 3, 0), (2, 52, 0), (1, 176, 0), (2, 240, 0)])
+def test_random_and_adversarial_llrs(gpu, bg, z, cpb):
+    """Heavy-tailed LLRs with exact zeros, -0.0, +-inf, NaN and magnitudes
+    above the 1000.0 two-min start value."""
+    dec = make_decoder(bg, z, max_batch=32, cw_per_cta=cpb)
+    oc = oracle_for(dec)
+    rng = np.random.default_rng(z * 10 + bg)
+    n = 11
+    llr = (rng.standard_t(3, size=(n, dec.n_bp)) * 3 + 0.8).astype(np.float32)
+    llr[:, :2 * z] = 0.0
+    m = rng.random(llr.shape)
+    llr[m < 0.002] = -0.0
+    llr[(m > 0.002) & (m < 0.003)] = np.inf
+    llr[(m > 0.003) & (m < 0.0035)] = -np.inf
+    llr[(m > 0.0035) & (m < 0.004)] = np.nan
+    llr[(m > 0.004) & (m < 0.01)] *= 5000.0
+    d = torch.from_numpy(llr).to(gpu)
+    for it in (1, 3, 7):
+        pk, app = dec.decode(d, it, want_app=True)
+        torch.cuda.synchronize()
+        opk, oapp, _ = oc.minsum_f32(llr, it, want_app=True)
+        np.testing.assert_array_equal(pk.cpu().numpy(), opk)
+        np.testing.assert_array_equal(bits_nan_canonical(app.cpu().numpy()), bits_nan_canonical(oapp))
+
+
+@pytest.mark.parametrize("bg,z,ebn0", [(1, 384, 2.0), (2, 128, 2.0), (1, 64, 2.5), (2, 20, 3.0)])
+def test_early_stop_parity(gpu, bg, z, ebn0):
+    dec = make_decoder(bg, z, max_batch=64)
+    oc = oracle_for(dec)
+    rate = dec.kb / (dec.cols - 2)
+    sig = np.full(24, codes.noise_sigma(ebn0, rate), np.float32)
+    llr, cw = oc.gen_llr(dec.kb, 77, 0, sig, 2)
+    pk, app, its = dec.decode(torch.from_numpy(llr).to(gpu), 12, early_stop=True, want_app=True,
+                              want_iters=True)
+    torch.cuda.synchronize()
+    opk, oapp, oits = oc.minsum_f32(llr, 12, early_stop=True, want_app=True)
+    np.testing.assert_array_equal(its.cpu().numpy(), oits)
+    np.testing.assert_array_equal(pk.cpu().numpy(), opk)
+    np.testing.assert_array_equal(app.cpu().numpy().view(np.uint32), oapp.view(np.uint32))
+    assert (oits < 12).any()
+    for i in np.nonzero(oits < 12)[0]:
+        assert oc.syndrome_weight(opk[i]) == 0
+
+
+def test_host_buffer_call_matches_device_call(gpu):
+    dec = Decoder(bg=1, z=384, max_batch=40)
+    sig = torch.full((40,), codes.noise_sigma(1.75, 1 / 3), device=gpu)
+    llr, _ = dec.gen_llr(5, 0, sig)
+    ref = dec.decode(llr, 10)
+    h_llr = llr.cpu().pin_memory()
+    h_out = torch.empty((40, dec.packed_bytes), dtype=torch.uint8).pin_memory()
+    s = torch.cuda.Stream()
+    dec.decode_host(h_llr, h_out, 10, stream=s)
+    s.synchronize()
+    assert torch.equal(h_out, ref.cpu())
+
+
+def test_errors_and_empty_batch(gpu):
+    dec = Decoder(bg=2, z=64, max_batch=8)
+    llr = torch.zeros((9, dec.n_bp), device=gpu)
+    with pytest.raises(_lib.NrLdpcError) as e:
+        dec.decode(llr, 5)
+    assert e.value.status == -5
+    out = dec.decode(llr[:0], 5)
+    assert out.shape == (0, dec.packed_bytes)
+    flat = torch.zeros(dec.n_bp * 2 + 1, device=gpu)
+    with pytest.raises(_lib.NrLdpcError) as e:
+        dec.decode(flat[1:].view(2, dec.n_bp), 5)
+    assert e.value.status == -4
+    with pytest.raises(_lib.NrLdpcError) as e:
+        Decoder(bg=1, z=17)
+    assert e.value.status == -2
+    lib = _lib.load()
+    assert lib.nrldpc_decode(None, None, None, 1, 1, 0, None, None, None) == -1
+    with pytest.raises(_lib.NrLdpcError):
+        dec.decode(llr[:2], 0)
+
+
+def test_full_size_batch_properties(gpu):
+    """4096 BG1 Z=384 codewords: noiseless codewords decode to themselves in
+    two iterations, high-SNR batches decode without errors, and sampled
+    codewords match the oracle bit for bit."""
+    n = 4096
+    dec = Decoder(bg=1, z=384, max_batch=n)
+    sig = torch.full((n,), codes.noise_sigma(3.0, 1 / 3), device=gpu)
+    llr, cw = dec.gen_llr(31, 1000, sig)
+    bits = torch.from_numpy(np.unpackbits(cw.cpu().numpy(), axis=1, bitorder="little")).to(gpu)
+    clean = (1.0 - 2.0 * bits.float()) * 8.0
+    clean[:, :768] = 0.0
+    pk = dec.decode(clean.contiguous(), 2)
+    counts = dec.count_errors(pk, cw)
+    torch.cuda.synchronize()
+    assert counts.tolist() == [0, 0]
+    pk = dec.decode(llr, 10)
+    counts = dec.count_errors(pk, cw)
+    torch.cuda.synchronize()
+    assert counts.tolist() == [0, 0]
+    oc = oracle_for(dec)
+    idx = [0, 1, 2047, 4095]
+    opk, _, _ = oc.minsum_f32(llr[idx].cpu().numpy(), 10)
+    np.testing.assert_array_equal(pk[idx].cpu().numpy(), opk)
+
+
+def test_count_errors_against_numpy(gpu):
+    dec = Decoder(bg=2, z=9, max_batch=64)
+    rng = np.random.default_rng(0)
+    a = rng.integers(0, 256, (50, dec.packed_bytes), dtype=np.uint8)
+    b = a.copy()
+    b[rng.random(b.shape) < 0.01] ^= 0x10
+    counts = dec.count_errors(torch.from_numpy(a).to(gpu), torch.from_numpy(b).to(gpu), n_info=77)
+    torch.cuda.synchronize()
+    diff = np.unpackbits(a ^ b, axis=1, bitorder="little")[:, :77].sum(1)
+    assert counts.tolist() == [int(diff.sum()), int((diff > 0).sum())]
