@@ -117,6 +117,27 @@ int nrldpc_decode_weighted(nrldpc_handle* h, const float* d_llr, uint8_t* d_pack
                            int n_iter, int early_stop, float* d_app, int32_t* d_iters,
                            nrldpc_stream_t stream);
 
+/* ---- learned weighted min-sum training (no reference counterpart) ----------
+ * Model: R^t_e = w[t][e] * sign * min (weights per iteration t < n_iter and
+ * base edge e, shared by all lifted copies); posterior as the decoder;
+ * loss = loss_scale * sum over t = 1..n_iter, codewords, columns of
+ * softplus(-y * L^t), y = +1 for bit 0 (BCE on the posterior LLRs).
+ * The caller allocates d_workspace of nrldpc_wms_workspace_bytes (per-iteration
+ * compressed check-node states + loss gradient seeds + adjoint scratch). */
+int nrldpc_wms_workspace_bytes(nrldpc_handle* h, int n_cw, int n_iter, size_t* bytes);
+/* Unrolled forward: *d_loss += loss; d_app (may be NULL) gets L^{n_iter}. */
+int nrldpc_wms_forward(nrldpc_handle* h, const float* d_llr, const uint8_t* d_cw_packed, int n_cw,
+                       int n_iter, const float* d_weights, void* d_workspace, float loss_scale,
+                       double* d_loss, float* d_app, nrldpc_stream_t stream);
+/* Adjoint of the last forward on this workspace: d_grad[n_iter][n_edges] += dloss/dw.
+ * Check-node messages are rebuilt from the stored two-min states, not stored. */
+int nrldpc_wms_backward(nrldpc_handle* h, int n_cw, int n_iter, const float* d_weights,
+                        void* d_workspace, double* d_grad, nrldpc_stream_t stream);
+/* Adam on n parameters (bias-corrected, step >= 1), weights clamped >= w_min. */
+int nrldpc_adam_step(int n, float* d_w, const double* d_grad, float* d_m, float* d_v, int step,
+                     float lr, float beta1, float beta2, float eps, float w_min,
+                     nrldpc_stream_t stream);
+
 /* Seeded channel generator on the GPU (bit-identical to the CPU oracle's):
  * info bits (Philox4x32-10), encode, BPSK, AWGN sigma[i], LLR = 2y/sigma^2;
  * first n_punct_cols columns get LLR 0.  d_cw_packed may be NULL. */

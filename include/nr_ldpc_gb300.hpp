@@ -1,0 +1,73 @@
+// Header-only C++ convenience layer over the C ABI in nr_ldpc_gb300.h,
+// shaped after the reference's host calls (ctarver/NR_GPU_LDPC):
+//   setup_ldpc(A, rate, n_iterations)             src/nr_ldpc.h:14
+//   perform_gpu_ldpc_decoding<T>(d, h, g, I, s)   src/gpu_decoder_top.h:13-18
+// One Decoder stands for the reference's process-global decoder state
+// (constant memory + dev_mem), without the globals: several can coexist.
+// A Decoder serves one stream at a time; give each concurrent stream its own.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+
+#include "nr_ldpc_gb300.h"
+
+namespace nrldpc {
+
+inline void check(int status, const char* what) {
+    if (status != NRLDPC_OK)
+        throw std::runtime_error(std::string(what) + ": " + nrldpc_status_string(status));
+}
+
+// Mirror of setup_ldpc (src/nr_ldpc.cpp:31-230).
+inline nrldpc_ldpc_params setup_ldpc(int A, float rate, int n_iterations) {
+    nrldpc_ldpc_params p;
+    check(nrldpc_setup_ldpc(A, rate, n_iterations, &p), "setup_ldpc");
+    return p;
+}
+
+class Decoder {
+public:
+    // Replaces setup_dev_memory + setup_gpu_grid +
+    // put_h_compact_and_params_in_constant_memory (src/setup_exp.cu:102-166,286-313).
+    Decoder(const nrldpc_ldpc_params& p, int max_batch, float alpha = 0.75f, int device = 0) {
+        nrldpc_config cfg{p.bg_index, p.Z, max_batch, alpha, device, 0};
+        check(nrldpc_init(&cfg, &h_), "nrldpc_init");
+        check(nrldpc_geometry(h_, nullptr, nullptr, nullptr, nullptr, &n_bp_, &packed_bytes_),
+              "nrldpc_geometry");
+    }
+    ~Decoder() { nrldpc_destroy(h_); }
+    Decoder(const Decoder&) = delete;
+    Decoder& operator=(const Decoder&) = delete;
+
+    int n_bp() const { return n_bp_; }                  // N_before_puncture
+    int packed_bytes() const { return packed_bytes_; }  // per codeword
+    nrldpc_handle* handle() const { return h_; }
+
+    // perform_gpu_ldpc_decoding (src/gpu_decoder_top.cu:16-52): host LLRs of
+    // n_cw codewords in, packed hard decisions out, queued on `stream`
+    // (pinned buffers overlap with other streams); the caller synchronizes.
+    void perform_gpu_ldpc_decoding(const float* h_llr, uint8_t* h_packed, int n_cw,
+                                   int n_iterations, cudaStream_t stream, bool early_stop = false) {
+        check(nrldpc_decode_host_async(h_, h_llr, h_packed, n_cw, n_iterations, early_stop ? 1 : 0,
+                                       reinterpret_cast<nrldpc_stream_t>(stream)),
+              "perform_gpu_ldpc_decoding");
+    }
+
+    // Device-resident variant (no copies).
+    void decode(const float* d_llr, uint8_t* d_packed, int n_cw, int n_iterations,
+                cudaStream_t stream, bool early_stop = false) {
+        check(nrldpc_decode(h_, d_llr, d_packed, n_cw, n_iterations, early_stop ? 1 : 0, nullptr,
+                            nullptr, reinterpret_cast<nrldpc_stream_t>(stream)),
+              "nrldpc_decode");
+    }
+
+private:
+    nrldpc_handle* h_ = nullptr;
+    int n_bp_ = 0, packed_bytes_ = 0;
+};
+
+}  // namespace nrldpc

@@ -50,6 +50,10 @@ SIGNATURES = {
     "nrldpc_decode_host_async": (_i, [_vp, _vp, _vp, _i, _i, _i, _vp]),
     "nrldpc_set_weights": (_i, [_vp, _vp, _i]),
     "nrldpc_decode_weighted": (_i, [_vp, _vp, _vp, _i, _i, _i, _vp, _vp, _vp]),
+    "nrldpc_wms_workspace_bytes": (_i, [_vp, _i, _i, C.POINTER(C.c_size_t)]),
+    "nrldpc_wms_forward": (_i, [_vp, _vp, _vp, _i, _i, _vp, _vp, _f, _vp, _vp, _vp]),
+    "nrldpc_wms_backward": (_i, [_vp, _i, _i, _vp, _vp, _vp, _vp]),
+    "nrldpc_adam_step": (_i, [_i, _vp, _vp, _vp, _vp, _i, _f, _f, _f, _f, _f, _vp]),
     "nrldpc_gen_llr": (_i, [_vp, _u64, _u64, _i, _vp, _i, _vp, _vp, _vp]),
     "nrldpc_count_errors": (_i, [_vp, _vp, _vp, _i, _i, _vp, _vp]),
     "nrldpc_device_error": (_i, [_vp]),

@@ -35,6 +35,7 @@ struct Handle {
     uint8_t* stage_packed = nullptr;
     float* weights = nullptr;
     int n_w_iters = 0;
+    bool wms_ready = false;
 };
 
 int map_cuda(cudaError_t e) { return e == cudaSuccess ? NRLDPC_OK : NRLDPC_ERR_CUDA; }
@@ -182,9 +183,9 @@ int init_impl(const int* base, int rows, int cols, int kb, const nrldpc_config* 
 
 int decode_impl(Handle* h, const float* llr, uint8_t* packed, int n_cw, int n_iter, int early,
                 float* app, int32_t* iters, bool weighted, cudaStream_t stream) {
-    if (!h || !llr || !packed || n_cw < 0 || n_iter < 1 || (early != 0 && early != 1))
-        return NRLDPC_ERR_INVALID_ARG;
-    if (n_cw == 0) return NRLDPC_OK;
+    if (!h || n_cw < 0 || n_iter < 1 || (early != 0 && early != 1)) return NRLDPC_ERR_INVALID_ARG;
+    if (n_cw == 0) return NRLDPC_OK;  // empty batch: nothing to read or write
+    if (!llr || !packed) return NRLDPC_ERR_INVALID_ARG;
     if (n_cw > h->max_batch) return NRLDPC_ERR_TOO_LARGE;
     if (reinterpret_cast<uintptr_t>(llr) % 16 != 0) return NRLDPC_ERR_ALIGNMENT;
     if (weighted && (!h->weights || h->n_w_iters < 1)) return NRLDPC_ERR_INVALID_ARG;
@@ -385,6 +386,83 @@ int nrldpc_set_weights(nrldpc_handle* handle, const float* w, int n_w_iters) {
     if (cudaMemcpy(h->weights, w, bytes, cudaMemcpyHostToDevice) != cudaSuccess) return NRLDPC_ERR_CUDA;
     h->n_w_iters = n_w_iters;
     return NRLDPC_OK;
+}
+
+// ---- learned weighted min-sum training --------------------------------------------------
+namespace {
+struct WmsLayout {
+    size_t states, gseed, gq, total;
+};
+WmsLayout wms_layout(const Handle* h, int n_cw, int n_iter) {
+    auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+    WmsLayout l;
+    const size_t rz = static_cast<size_t>(h->tab.rows) * h->tab.z;
+    l.states = up(static_cast<size_t>(n_iter) * n_cw * rz * sizeof(uint4));
+    l.gseed = up(static_cast<size_t>(n_iter) * n_cw * h->tab.n_bp * sizeof(float));
+    l.gq = up(static_cast<size_t>(h->sm_count) * h->cpb * rz * sizeof(uint4));
+    l.total = l.states + l.gseed + l.gq;
+    return l;
+}
+int wms_check(Handle* h, int n_cw, int n_iter) {
+    if (!h || n_cw < 1 || n_iter < 1) return NRLDPC_ERR_INVALID_ARG;
+    if (n_cw > h->max_batch) return NRLDPC_ERR_TOO_LARGE;
+    if (!h->wms_ready) {
+        if (wms_kernel_attributes(wms_smem_bytes(h->tab, h->cpb)) != cudaSuccess) return NRLDPC_ERR_CUDA;
+        h->wms_ready = true;
+    }
+    return NRLDPC_OK;
+}
+}  // namespace
+
+int nrldpc_wms_workspace_bytes(nrldpc_handle* handle, int n_cw, int n_iter, size_t* bytes) {
+    Handle* h = reinterpret_cast<Handle*>(handle);
+    if (!h || !bytes || n_cw < 1 || n_iter < 1) return NRLDPC_ERR_INVALID_ARG;
+    *bytes = wms_layout(h, n_cw, n_iter).total;
+    return NRLDPC_OK;
+}
+
+int nrldpc_wms_forward(nrldpc_handle* handle, const float* d_llr, const uint8_t* d_cw_packed, int n_cw,
+                       int n_iter, const float* d_weights, void* d_workspace, float loss_scale,
+                       double* d_loss, float* d_app, nrldpc_stream_t stream) {
+    Handle* h = reinterpret_cast<Handle*>(handle);
+    int rc = wms_check(h, n_cw, n_iter);
+    if (rc) return rc;
+    if (!d_llr || !d_cw_packed || !d_weights || !d_workspace || !d_loss) return NRLDPC_ERR_INVALID_ARG;
+    if (reinterpret_cast<uintptr_t>(d_llr) % 16 != 0) return NRLDPC_ERR_ALIGNMENT;
+    const WmsLayout l = wms_layout(h, n_cw, n_iter);
+    char* ws = static_cast<char*>(d_workspace);
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (cudaMemsetAsync(h->scratch, 0, sizeof(int), st) != cudaSuccess) return NRLDPC_ERR_CUDA;
+    return map_cuda(launch_wms(false, h->tab, d_llr, d_cw_packed, d_weights,
+                               reinterpret_cast<uint4*>(ws), reinterpret_cast<float*>(ws + l.states),
+                               reinterpret_cast<uint4*>(ws + l.states + l.gseed), d_loss, nullptr,
+                               d_app, h->scratch, n_cw, n_iter, h->cpb, h->sm_count, h->threads,
+                               wms_smem_bytes(h->tab, h->cpb), loss_scale, st));
+}
+
+int nrldpc_wms_backward(nrldpc_handle* handle, int n_cw, int n_iter, const float* d_weights,
+                        void* d_workspace, double* d_grad, nrldpc_stream_t stream) {
+    Handle* h = reinterpret_cast<Handle*>(handle);
+    int rc = wms_check(h, n_cw, n_iter);
+    if (rc) return rc;
+    if (!d_weights || !d_workspace || !d_grad) return NRLDPC_ERR_INVALID_ARG;
+    const WmsLayout l = wms_layout(h, n_cw, n_iter);
+    char* ws = static_cast<char*>(d_workspace);
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (cudaMemsetAsync(h->scratch, 0, sizeof(int), st) != cudaSuccess) return NRLDPC_ERR_CUDA;
+    return map_cuda(launch_wms(true, h->tab, nullptr, nullptr, d_weights, reinterpret_cast<uint4*>(ws),
+                               reinterpret_cast<float*>(ws + l.states),
+                               reinterpret_cast<uint4*>(ws + l.states + l.gseed), nullptr, d_grad,
+                               nullptr, h->scratch, n_cw, n_iter, h->cpb, h->sm_count, h->threads,
+                               wms_smem_bytes(h->tab, h->cpb), 0.0f, st));
+}
+
+int nrldpc_adam_step(int n, float* d_w, const double* d_grad, float* d_m, float* d_v, int step,
+                     float lr, float beta1, float beta2, float eps, float w_min,
+                     nrldpc_stream_t stream) {
+    if (n < 1 || !d_w || !d_grad || !d_m || !d_v || step < 1) return NRLDPC_ERR_INVALID_ARG;
+    return map_cuda(launch_adam(n, d_w, d_grad, d_m, d_v, step, lr, beta1, beta2, eps, w_min,
+                                reinterpret_cast<cudaStream_t>(stream)));
 }
 
 int nrldpc_gen_llr(nrldpc_handle* handle, uint64_t seed, uint64_t cw_base, int n_cw,

@@ -55,6 +55,16 @@ size_t decode_smem_bytes(const CodeTable& tab, int cpb);
 cudaError_t decode_kernel_attributes(size_t smem);
 int decode_max_ctas_per_sm(bool weighted, int minb, int threads, size_t smem);
 
+// Learned weighted min-sum training kernels (wms.cu).
+size_t wms_smem_bytes(const CodeTable& tab, int cpb);
+cudaError_t wms_kernel_attributes(size_t smem);
+cudaError_t launch_wms(bool backward, const CodeTable& tab, const float* llr, const uint8_t* cw,
+                       const float* weights, uint4* states, float* gseed, uint4* gq, double* loss,
+                       double* grad, float* app, int* counters, int n_cw, int T, int cpb, int grid,
+                       int threads, size_t smem, float scale, cudaStream_t stream);
+cudaError_t launch_adam(int n, float* w, const double* grad, float* m, float* v, int step, float lr,
+                        float b1, float b2, float eps, float w_min, cudaStream_t stream);
+
 // 5G NR (bg, z) code table, built on the caller's storage (no allocation).
 bool make_nr_table(int bg, int z, CodeTable* t);
 
