@@ -50,7 +50,8 @@ typedef enum {
     NRLDPC_ERR_TOO_LARGE = -5,     /* batch beyond the handle's max_batch */
     NRLDPC_ERR_TIMEOUT = -6,       /* a bounded device-side wait expired */
     NRLDPC_ERR_NO_MEMORY = -7,     /* host or device allocation failed */
-    NRLDPC_ERR_NO_DEVICE = -8      /* no CUDA device / wrong architecture */
+    NRLDPC_ERR_NO_DEVICE = -8,     /* no CUDA device / wrong architecture */
+    NRLDPC_ERR_SCRATCH_TOO_SMALL = -9 /* code needs more scratch than the fixed array holds */
 } nrldpc_status;
 
 /* Code parameters as the reference computes them (mirror of ldpc_params,
@@ -150,6 +151,21 @@ int nrldpc_gen_llr(nrldpc_handle* h, uint64_t seed, uint64_t cw_base, int n_cw,
 int nrldpc_count_errors(nrldpc_handle* h, const uint8_t* d_packed, const uint8_t* d_cw_packed,
                         int n_cw, int n_info, unsigned long long* d_counts,
                         nrldpc_stream_t stream);
+
+/* Decode without allocating anything (no reference counterpart).  For
+ * callers that cannot call cudaMalloc at decode time -- a physical-layer
+ * pipeline that reserves all device memory at start-up and must not allocate
+ * (allocation can block the device) while it processes slots, or code inside
+ * another runtime's memory manager -- and so cannot hold an nrldpc_handle.
+ * Same results as nrldpc_decode for 5G NR (bg, z) with alpha (device
+ * pointers, 16-byte aligned d_llr; packed output as nrldpc_decode).  Scratch
+ * is one static 42 MiB device array in the library, held by a GPU from the
+ * first call on it until the process exits; a code whose per-CTA check-node
+ * state does not fit returns NRLDPC_ERR_SCRATCH_TOO_SMALL.  The first call on
+ * a device (the current one) sets it up: make it before any stream capture.
+ * Calls share the array: calls that overlap on the GPU race; serialise them. */
+int nrldpc_decode_noalloc(int bg, int z, float alpha, const float* d_llr, uint8_t* d_packed,
+                          int n_cw, int n_iter, int early_stop, nrldpc_stream_t stream);
 
 /* Last device-side error recorded by a bounded wait (0 if none); clears it. */
 int nrldpc_device_error(nrldpc_handle* h);

@@ -56,6 +56,7 @@ SIGNATURES = {
     "nrldpc_adam_step": (_i, [_i, _vp, _vp, _vp, _vp, _i, _f, _f, _f, _f, _f, _vp]),
     "nrldpc_gen_llr": (_i, [_vp, _u64, _u64, _i, _vp, _i, _vp, _vp, _vp]),
     "nrldpc_count_errors": (_i, [_vp, _vp, _vp, _i, _i, _vp, _vp]),
+    "nrldpc_decode_noalloc": (_i, [_i, _i, _f, _vp, _vp, _i, _i, _i, _vp]),
     "nrldpc_device_error": (_i, [_vp]),
     "nrldpc_status_string": (C.c_char_p, [_i]),
 }

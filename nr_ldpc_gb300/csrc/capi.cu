@@ -509,6 +509,8 @@ const char* nrldpc_status_string(int status) {
         case NRLDPC_ERR_TIMEOUT: return "device-side wait timed out";
         case NRLDPC_ERR_NO_MEMORY: return "allocation failed";
         case NRLDPC_ERR_NO_DEVICE: return "no usable CUDA device";
+        case NRLDPC_ERR_SCRATCH_TOO_SMALL:
+            return "code needs more check-node scratch than the fixed no-alloc array holds";
         default: return "unknown status";
     }
 }
