@@ -61,6 +61,8 @@ bool fill_table(const int* base, int rows, int cols, int z, int kb, CodeTable* t
             if (v < 0 || e >= kMaxEdges) return false;
             const int sh = v % z;
             t->edge[e] = static_cast<uint32_t>(c * z + sh) | (static_cast<uint32_t>(z - sh) << 16);
+            t->ebase4[e] = static_cast<uint32_t>(c * z + sh) * 4u;
+            t->ethr[e] = static_cast<uint16_t>(z - sh);
             t->edge_col[e] = static_cast<uint8_t>(c);
             t->edge_shift[e] = static_cast<uint16_t>(sh);
             e++;

@@ -86,26 +86,37 @@ __device__ __forceinline__ void fence_proxy_async() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
+// 32-bit shared-memory accesses by byte address.  Volatile keeps them in
+// program order; within a row every posterior load precedes every store, and
+// rows between barriers touch disjoint columns.
+__device__ __forceinline__ float lds(uint32_t a) {
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(a));
+    return v;
+}
+__device__ __forceinline__ void sts(uint32_t a, float v) {
+    asm volatile("st.shared.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
+}
+
 // One lifted row (base row with D edges, sub-row s) of one iteration.
 // The first iteration passes a zero state (and a zero previous weight), so
 // R_old = +0 and Q = L - (+0) = L, dt = R - (+0) = R exactly, as in
 // cnp_kernel_1st_iter.  CHECK also accumulates the parity of the hard
 // decisions read from Lold (syndrome of the previous iteration).
+//   s4old: shared byte address of this slot's Lold plus 4*s;
+//   dnew:  byte distance from Lold to Lnew; z4 = 4*Z.
 template <int D, bool WEIGHTED, bool CHECK>
-__device__ __forceinline__ void row_update(const CodeTable& tab, int e0, uint32_t s,
-                                           const float* __restrict__ lold, float* lnew,
-                                           const float2* wpair, uint4 st, uint4* st_out,
-                                           float alpha, uint32_t& syn) {
-    const uint32_t z = static_cast<uint32_t>(tab.z);
+__device__ __forceinline__ void row_update(const CodeTable& tab, int e0, uint32_t s, uint32_t s4old,
+                                           uint32_t dnew, uint32_t z4, const float2* wpair, uint4 st,
+                                           uint4* st_out, float alpha, uint32_t& syn) {
     uint32_t addr[D];
     float lv[D];
 #pragma unroll
     for (int i = 0; i < D; i++) {
-        const uint32_t ed = tab.edge[e0 + i];
-        uint32_t a = s + (ed & 0xffffu);
-        if (s >= (ed >> 16)) a -= z;  // (s + V) mod Z
+        uint32_t a = s4old + tab.ebase4[e0 + i];
+        if (s >= tab.ethr[e0 + i]) a -= z4;  // column (s + V) mod Z of the edge's block
         addr[i] = a;
-        lv[i] = lold[a];
+        lv[i] = lds(a);
     }
     // old messages R_old from the previous iteration's state
     float rold[D];
@@ -147,7 +158,7 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, uint32_
     }
     float nv[D];
 #pragma unroll
-    for (int i = 0; i < D; i++) nv[i] = lnew[addr[i]];
+    for (int i = 0; i < D; i++) nv[i] = lds(addr[i] + dnew);
 #pragma unroll
     for (int i = 0; i < D; i++) {
         float mag;
@@ -157,22 +168,23 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, uint32_
             mag = i == idx ? a2 : a1;
         const float rn = __uint_as_float(__float_as_uint(mag) | ((rsign << (31 - i)) & 0x80000000u));
         const float dt = __fsub_rn(rn, rold[i]);
-        lnew[addr[i]] = __fadd_rn(nv[i], dt);
+        sts(addr[i] + dnew, __fadd_rn(nv[i], dt));
     }
-    if (st_out) {
-        const uint32_t info = static_cast<uint32_t>(idx) | ((rsign & ((1u << D) - 1u)) << 8);
-        __stcg(st_out, make_uint4(__float_as_uint(m1), __float_as_uint(m2), info, 0u));
-    }
+    // stored every iteration (the last one's is never read)
+    const uint32_t info = static_cast<uint32_t>(idx) | ((rsign & ((1u << D) - 1u)) << 8);
+    __stcg(st_out, make_uint4(__float_as_uint(m1), __float_as_uint(m2), info, 0u));
 }
 
 template <bool WEIGHTED, bool CHECK>
 __device__ __forceinline__ void row_dispatch(int deg, const CodeTable& tab, int e0, uint32_t s,
-                                             const float* lold, float* lnew, const float2* wpair,
-                                             uint4 st, uint4* st_out, float alpha, uint32_t& syn) {
+                                             uint32_t s4old, uint32_t dnew, uint32_t z4,
+                                             const float2* wpair, uint4 st, uint4* st_out,
+                                             float alpha, uint32_t& syn) {
     switch (deg) {
-#define NRLDPC_ROW_CASE(D)                                                                   \
-    case D:                                                                                  \
-        row_update<D, WEIGHTED, CHECK>(tab, e0, s, lold, lnew, wpair, st, st_out, alpha, syn); \
+#define NRLDPC_ROW_CASE(D)                                                                 \
+    case D:                                                                                \
+        row_update<D, WEIGHTED, CHECK>(tab, e0, s, s4old, dnew, z4, wpair, st, st_out, alpha, \
+                                       syn);                                               \
         break;
         NRLDPC_ROW_CASE(1) NRLDPC_ROW_CASE(2) NRLDPC_ROW_CASE(3) NRLDPC_ROW_CASE(4)
         NRLDPC_ROW_CASE(5) NRLDPC_ROW_CASE(6) NRLDPC_ROW_CASE(7) NRLDPC_ROW_CASE(8)
@@ -206,25 +218,35 @@ __device__ __forceinline__ void write_outputs(const CodeTable& tab, const float*
 }
 
 // All base rows of one iteration, ascending; returns the OR of the row
-// parities of the hard decisions read (CHECK only).
+// parities of the hard decisions read (CHECK only).  The check-node state of
+// row r+3 is requested while row r runs (L2 latency spans several rows).
 template <bool WEIGHTED, bool CHECK>
-__device__ __forceinline__ uint32_t iterate_rows(const CodeTable& tab, uint32_t s, const float* lold,
-                                                 float* lnew, const float2* wpair, uint4* st_base,
-                                                 bool act, bool first, bool last, float alpha) {
+__device__ __forceinline__ uint32_t iterate_rows(const CodeTable& tab, uint32_t s, uint32_t s4old,
+                                                 uint32_t dnew, const float2* wpair, uint4* st_base,
+                                                 bool act, bool first, float alpha) {
     const int z = tab.z, rows = tab.rows;
+    const uint32_t z4 = 4u * static_cast<uint32_t>(z);
     uint32_t fail = 0;
-    uint4 st_cur = make_uint4(0u, 0u, 0u, 0u);
-    if (!first && act) st_cur = __ldcg(st_base + s);
+    const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+    const bool pf = !first && act;
+    uint4 s0 = zero, s1 = zero, s2 = zero;
+    if (pf) {
+        s0 = __ldcg(st_base + s);
+        s1 = __ldcg(st_base + min(1, rows - 1) * z + s);
+        s2 = __ldcg(st_base + min(2, rows - 1) * z + s);
+    }
     for (int r = 0; r < rows; r++) {
-        uint4 st_next = make_uint4(0u, 0u, 0u, 0u);
-        if (!first && act && r + 1 < rows) st_next = __ldcg(st_base + (r + 1) * z + s);
+        uint4 s3 = zero;
+        if (pf) s3 = __ldcg(st_base + min(r + 3, rows - 1) * z + s);
         if (act) {
             uint32_t syn = 0;
-            row_dispatch<WEIGHTED, CHECK>(tab.row_deg[r], tab, tab.row_ptr[r], s, lold, lnew, wpair,
-                                          st_cur, last ? nullptr : st_base + r * z + s, alpha, syn);
+            row_dispatch<WEIGHTED, CHECK>(tab.row_deg[r], tab, tab.row_ptr[r], s, s4old, dnew, z4,
+                                          wpair, s0, st_base + r * z + s, alpha, syn);
             fail |= syn;
         }
-        st_cur = st_next;
+        s0 = s1;
+        s1 = s2;
+        s2 = s3;
         if (tab.sync_after[r]) __syncthreads();
     }
     return fail;
@@ -283,8 +305,13 @@ __global__ void __launch_bounds__(kMaxThreads, MINB)
 
         bool slot_done = !valid_thread || slot >= n_valid;
         const int cw = cw0 + slot;
-        float* lold = buf0 + static_cast<size_t>(slot) * n;  // per-slot views
-        float* lnew = buf1 + static_cast<size_t>(slot) * n;
+        float* lold = buf0 + static_cast<size_t>(slot) * n;  // read by the check-node pass
+        float* lnew = buf1 + static_cast<size_t>(slot) * n;  // accumulates the new posterior
+        const uint32_t s4old = smem_addr(lold) + 4u * s;
+        const uint32_t dnew = static_cast<uint32_t>(cpb) * static_cast<uint32_t>(n) * 4u;
+        if (!slot_done)
+            for (int k = static_cast<int>(s); k < n / 4; k += z)
+                reinterpret_cast<float4*>(lnew)[k] = reinterpret_cast<const float4*>(lold)[k];
         for (int t = 0; t < a.n_iter; t++) {
             const bool first = t == 0, last = t == a.n_iter - 1;
             if (WEIGHTED) {
@@ -295,19 +322,14 @@ __global__ void __launch_bounds__(kMaxThreads, MINB)
                                            a.weights[tc * tab.n_edges + e]);
             }
             if (tid < cpb) s_fail[tid] = 0;
-            if (!slot_done) {  // Lnew starts as Lold
-                const float4* src = reinterpret_cast<const float4*>(lold);
-                float4* dst = reinterpret_cast<float4*>(lnew);
-                for (int k = static_cast<int>(s); k < n / 4; k += z) dst[k] = src[k];
-            }
             __syncthreads();
             const bool act = !slot_done;
             const bool check = a.early_stop && t > 0;
             const uint32_t fail =
-                check ? iterate_rows<WEIGHTED, true>(tab, s, lold, lnew, wpair, st_base, act, first,
-                                                    last, a.alpha)
-                      : iterate_rows<WEIGHTED, false>(tab, s, lold, lnew, wpair, st_base, act,
-                                                     first, last, a.alpha);
+                check ? iterate_rows<WEIGHTED, true>(tab, s, s4old, dnew, wpair, st_base, act, first,
+                                                    a.alpha)
+                      : iterate_rows<WEIGHTED, false>(tab, s, s4old, dnew, wpair, st_base, act, first,
+                                                     a.alpha);
             if (check) {
                 if (act && fail) atomicOr(&s_fail[slot], 1);
                 __syncthreads();
@@ -320,14 +342,16 @@ __global__ void __launch_bounds__(kMaxThreads, MINB)
                 slot_done = slot_done || conv;
                 if (__syncthreads_and(slot_done)) break;
             }
-            float* tmp = lold;  // the posterior just accumulated is next iteration's input
-            lold = lnew;
-            lnew = tmp;
-            if (last && !slot_done) {
-                write_outputs(tab, lold, s, a.packed + static_cast<size_t>(cw) * tab.packed_bytes,
-                              a.app ? a.app + static_cast<size_t>(cw) * n : nullptr,
-                              a.iters ? a.iters + cw : nullptr, a.n_iter);
+            if (last) {
+                if (!slot_done)
+                    write_outputs(tab, lnew, s, a.packed + static_cast<size_t>(cw) * tab.packed_bytes,
+                                  a.app ? a.app + static_cast<size_t>(cw) * n : nullptr,
+                                  a.iters ? a.iters + cw : nullptr, a.n_iter);
+                break;
             }
+            if (!slot_done)  // the posterior just accumulated is the next iteration's input
+                for (int k = static_cast<int>(s); k < n / 4; k += z)
+                    reinterpret_cast<float4*>(lold)[k] = reinterpret_cast<const float4*>(lnew)[k];
         }
         __syncthreads();  // buffers are rewritten by the next group's copy
     }

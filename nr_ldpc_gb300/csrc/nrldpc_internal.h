@@ -25,6 +25,11 @@ struct CodeTable {
     // per edge, row-major ascending (row, then column) = the reference's
     // h_compact1 order: low 16 bits blk_col*Z + V, high 16 bits Z - V
     uint32_t edge[kMaxEdges];
+    // the same edge as byte offset (blk_col*Z + V)*4 into a posterior buffer
+    // and wrap threshold Z - V: the sub-row s column is at s*4 + ebase4,
+    // minus 4Z when s >= ethr
+    uint32_t ebase4[kMaxEdges];
+    uint16_t ethr[kMaxEdges];
     uint8_t edge_col[kMaxEdges];
     uint16_t edge_shift[kMaxEdges];  // V mod Z
 };
