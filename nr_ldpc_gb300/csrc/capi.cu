@@ -29,7 +29,7 @@ struct Handle {
     int max_batch = 0;
     int cpb = 1, threads = 32, ctas_per_sm = 1, sm_count = 1, max_grid = 1, minb = 1;
     size_t smem = 0;
-    uint4* state = nullptr;
+    uint32_t* state = nullptr;
     int* scratch = nullptr;  // [0] work counter, [1] error flag
     float* stage_llr = nullptr;
     uint8_t* stage_packed = nullptr;
@@ -171,7 +171,7 @@ int init_impl(const int* base, int rows, int cols, int kb, const nrldpc_config* 
     const size_t state_elems =
         static_cast<size_t>(h->max_grid) * cpb * h->tab.rows * static_cast<size_t>(z);
     const size_t n_llr = static_cast<size_t>(cfg->max_batch) * h->tab.n_bp;
-    if (cudaMalloc(&h->state, state_elems * sizeof(uint4)) != cudaSuccess ||
+    if (cudaMalloc(&h->state, state_elems * kStateBytesPerRow) != cudaSuccess ||
         cudaMalloc(&h->scratch, 64) != cudaSuccess || cudaMemset(h->scratch, 0, 64) != cudaSuccess ||
         cudaMalloc(&h->stage_llr, n_llr * sizeof(float)) != cudaSuccess ||
         cudaMalloc(&h->stage_packed,

@@ -3,10 +3,11 @@
 // One CTA holds `cpb` whole codewords on chip for all iterations:
 //   * two fp32 posterior buffers per codeword in shared memory, Lold (read by
 //     the check-node pass) and Lnew (accumulates the posterior update);
-//   * the check-node state between iterations, compressed to 16 B per lifted
-//     row (min1, min2, argmin, R sign bits), in a per-CTA slot of global
-//     memory that stays L2-resident (each CTA reuses its slot for every
-//     codeword it takes), streamed with 128-bit loads one row ahead.
+//   * the check-node state between iterations, compressed to 12 B per lifted
+//     row (min1, min2, argmin + R sign bits) as three coalesced word streams,
+//     in a per-CTA slot of global memory that stays L2-resident (each CTA
+//     reuses its slot for every codeword it takes), requested three rows
+//     ahead.
 // The LLR batch comes into shared memory with one cp.async.bulk copy per
 // codeword group (mbarrier completion, bounded wait).
 //
@@ -105,10 +106,13 @@ __device__ __forceinline__ void sts(uint32_t a, float v) {
 // decisions read from Lold (syndrome of the previous iteration).
 //   s4old: shared byte address of this slot's Lold plus 4*s;
 //   dnew:  byte distance from Lold to Lnew; z4 = 4*Z.
+//   st: this row's state from the previous iteration; st_out: where this
+//   iteration's goes (min1, then min2 and info at +rz and +2*rz words), or
+//   null in the last iteration.
 template <int D, bool WEIGHTED, bool CHECK>
 __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, uint32_t s, uint32_t s4old,
-                                           uint32_t dnew, uint32_t z4, const float2* wpair, uint4 st,
-                                           uint4* st_out, float alpha, uint32_t& syn) {
+                                           uint32_t dnew, uint32_t z4, const float2* wpair, uint3 st,
+                                           uint32_t* st_out, uint32_t rz, float alpha, uint32_t& syn) {
     uint32_t addr[D];
     float lv[D];
 #pragma unroll
@@ -170,21 +174,24 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, uint32_
         const float dt = __fsub_rn(rn, rold[i]);
         sts(addr[i] + dnew, __fadd_rn(nv[i], dt));
     }
-    // stored every iteration (the last one's is never read)
-    const uint32_t info = static_cast<uint32_t>(idx) | ((rsign & ((1u << D) - 1u)) << 8);
-    __stcg(st_out, make_uint4(__float_as_uint(m1), __float_as_uint(m2), info, 0u));
+    if (st_out) {
+        const uint32_t info = static_cast<uint32_t>(idx) | ((rsign & ((1u << D) - 1u)) << 8);
+        __stcg(st_out, __float_as_uint(m1));
+        __stcg(st_out + rz, __float_as_uint(m2));
+        __stcg(st_out + 2 * rz, info);
+    }
 }
 
 template <bool WEIGHTED, bool CHECK>
 __device__ __forceinline__ void row_dispatch(int deg, const CodeTable& tab, int e0, uint32_t s,
                                              uint32_t s4old, uint32_t dnew, uint32_t z4,
-                                             const float2* wpair, uint4 st, uint4* st_out,
-                                             float alpha, uint32_t& syn) {
+                                             const float2* wpair, uint3 st, uint32_t* st_out,
+                                             uint32_t rz, float alpha, uint32_t& syn) {
     switch (deg) {
-#define NRLDPC_ROW_CASE(D)                                                                 \
-    case D:                                                                                \
-        row_update<D, WEIGHTED, CHECK>(tab, e0, s, s4old, dnew, z4, wpair, st, st_out, alpha, \
-                                       syn);                                               \
+#define NRLDPC_ROW_CASE(D)                                                                   \
+    case D:                                                                                  \
+        row_update<D, WEIGHTED, CHECK>(tab, e0, s, s4old, dnew, z4, wpair, st, st_out, rz, alpha, \
+                                       syn);                                                 \
         break;
         NRLDPC_ROW_CASE(1) NRLDPC_ROW_CASE(2) NRLDPC_ROW_CASE(3) NRLDPC_ROW_CASE(4)
         NRLDPC_ROW_CASE(5) NRLDPC_ROW_CASE(6) NRLDPC_ROW_CASE(7) NRLDPC_ROW_CASE(8)
@@ -217,31 +224,37 @@ __device__ __forceinline__ void write_outputs(const CodeTable& tab, const float*
     if (iters && s == 0) *iters = it;
 }
 
+__device__ __forceinline__ uint3 load_state(const uint32_t* p, uint32_t rz) {
+    return make_uint3(__ldcg(p), __ldcg(p + rz), __ldcg(p + 2 * rz));
+}
+
 // All base rows of one iteration, ascending; returns the OR of the row
 // parities of the hard decisions read (CHECK only).  The check-node state of
 // row r+3 is requested while row r runs (L2 latency spans several rows).
+// State layout per CTA slot: min1[rows*Z], min2[rows*Z], info[rows*Z].
 template <bool WEIGHTED, bool CHECK>
 __device__ __forceinline__ uint32_t iterate_rows(const CodeTable& tab, uint32_t s, uint32_t s4old,
-                                                 uint32_t dnew, const float2* wpair, uint4* st_base,
-                                                 bool act, bool first, float alpha) {
+                                                 uint32_t dnew, const float2* wpair, uint32_t* st_base,
+                                                 bool act, bool first, bool last, float alpha) {
     const int z = tab.z, rows = tab.rows;
-    const uint32_t z4 = 4u * static_cast<uint32_t>(z);
+    const uint32_t z4 = 4u * static_cast<uint32_t>(z), rz = static_cast<uint32_t>(rows * z);
     uint32_t fail = 0;
-    const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+    const uint3 zero = make_uint3(0u, 0u, 0u);
     const bool pf = !first && act;
-    uint4 s0 = zero, s1 = zero, s2 = zero;
+    uint3 s0 = zero, s1 = zero, s2 = zero;
     if (pf) {
-        s0 = __ldcg(st_base + s);
-        s1 = __ldcg(st_base + min(1, rows - 1) * z + s);
-        s2 = __ldcg(st_base + min(2, rows - 1) * z + s);
+        s0 = load_state(st_base + s, rz);
+        s1 = load_state(st_base + min(1, rows - 1) * z + s, rz);
+        s2 = load_state(st_base + min(2, rows - 1) * z + s, rz);
     }
     for (int r = 0; r < rows; r++) {
-        uint4 s3 = zero;
-        if (pf) s3 = __ldcg(st_base + min(r + 3, rows - 1) * z + s);
+        uint3 s3 = zero;
+        if (pf) s3 = load_state(st_base + min(r + 3, rows - 1) * z + s, rz);
         if (act) {
             uint32_t syn = 0;
             row_dispatch<WEIGHTED, CHECK>(tab.row_deg[r], tab, tab.row_ptr[r], s, s4old, dnew, z4,
-                                          wpair, s0, st_base + r * z + s, alpha, syn);
+                                          wpair, s0, last ? nullptr : st_base + r * z + s, rz,
+                                          alpha, syn);
             fail |= syn;
         }
         s0 = s1;
@@ -272,8 +285,8 @@ __global__ void __launch_bounds__(kMaxThreads, MINB)
     const bool valid_thread = slot < cpb;
     float* buf0 = bufs;
     float* buf1 = bufs + static_cast<size_t>(cpb) * n;
-    uint4* st_base =
-        a.state + (static_cast<size_t>(blockIdx.x) * cpb + (valid_thread ? slot : 0)) * rows * z;
+    uint32_t* st_base =
+        a.state + (static_cast<size_t>(blockIdx.x) * cpb + (valid_thread ? slot : 0)) * 3 * rows * z;
 
     if (tid == 0) {
         mbar_init(bar, 1);
@@ -327,9 +340,9 @@ __global__ void __launch_bounds__(kMaxThreads, MINB)
             const bool check = a.early_stop && t > 0;
             const uint32_t fail =
                 check ? iterate_rows<WEIGHTED, true>(tab, s, s4old, dnew, wpair, st_base, act, first,
-                                                    a.alpha)
+                                                    last, a.alpha)
                       : iterate_rows<WEIGHTED, false>(tab, s, s4old, dnew, wpair, st_base, act, first,
-                                                     a.alpha);
+                                                     last, a.alpha);
             if (check) {
                 if (act && fail) atomicOr(&s_fail[slot], 1);
                 __syncthreads();

@@ -10,9 +10,9 @@
 // passes only its input and output buffers, and the decoder's scratch lives in
 // a fixed static device array of this file.
 //
-// Scratch: kNoAllocScratchBytes (42 MiB) for the check-node state of the
+// Scratch: kNoAllocScratchBytes (32 MiB) for the check-node state of the
 // persistent decode CTAs, enough for one CTA per SM of a 152-SM GB300 at the
-// largest code (BG1, Z = 384: 282,624 bytes per CTA), plus 256 bytes of
+// largest code (BG1, Z = 384: 211,968 bytes per CTA), plus 256 bytes of
 // counters.  A GPU holds this memory from the first call of this entry point
 // on it (module load) until the process exits.
 //
@@ -35,7 +35,7 @@
 namespace nrldpc {
 namespace {
 
-constexpr size_t kNoAllocScratchBytes = size_t(42) << 20;
+constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;
 constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_state[kNoAllocScratchBytes];
@@ -44,7 +44,7 @@ static __device__ __align__(256) int g_noalloc_counters[64];  // [0] scheduler, 
 struct DeviceSetup {
     bool done;
     int status;
-    uint4* state;
+    uint32_t* state;
     int* counters;
     int sm_count;
     size_t smem_optin;
@@ -67,7 +67,7 @@ int setup_device(int dev, DeviceSetup** out) {
             cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
             s.status = NRLDPC_ERR_CUDA;
         } else {
-            s.state = static_cast<uint4*>(p);
+            s.state = static_cast<uint32_t*>(p);
             s.counters = static_cast<int*>(q);
             s.sm_count = prop.multiProcessorCount;
             s.smem_optin = prop.sharedMemPerBlockOptin;
@@ -107,7 +107,7 @@ extern "C" int nrldpc_decode_noalloc(int bg, int z, float alpha, const float* d_
     const int threads = (cpb * z + 31) / 32 * 32;
     const int minb = (2 * (smem + 1024) <= s->smem_per_sm) ? 2 : 1;
     const int per_sm = decode_max_ctas_per_sm(false, minb, threads, smem);
-    const size_t slot_bytes = static_cast<size_t>(cpb) * tab.rows * tab.z * sizeof(uint4);
+    const size_t slot_bytes = static_cast<size_t>(cpb) * tab.rows * tab.z * kStateBytesPerRow;
     const size_t slots = kNoAllocScratchBytes / slot_bytes;
     if (slots < 1) return NRLDPC_ERR_SCRATCH_TOO_SMALL;
     DecodeArgs a{};

@@ -34,15 +34,16 @@ struct CodeTable {
     uint16_t edge_shift[kMaxEdges];  // V mod Z
 };
 
-// Check-node state of one lifted row, kept between iterations (16 B):
-//   x = min1 (raw |Q|), y = min2, z = idx (bits 0..4) | R sign of edge i at
-//   bit 8+i, w = unused.
+// Check-node state of one lifted row, kept between iterations (12 B): min1
+// (raw |Q|), min2, info = idx (bits 0..4) | R sign of edge i at bit 8+i,
+// stored as three arrays per CTA slot: [slot][3][rows * Z] words.
+constexpr size_t kStateBytesPerRow = 12;
 struct DecodeArgs {
     const float* llr;
     uint8_t* packed;
     float* app;
     int32_t* iters;
-    uint4* state;           // [grid * cpb][rows * Z]
+    uint32_t* state;        // [grid * cpb][3][rows * Z]
     int* work_counter;      // dynamic codeword-group scheduler, zeroed per launch
     int* error_flag;        // bounded-wait failures
     const float* weights;   // [n_w_iters][n_edges] or null
