@@ -152,6 +152,50 @@ int nrldpc_count_errors(nrldpc_handle* h, const uint8_t* d_packed, const uint8_t
                         int n_cw, int n_info, unsigned long long* d_counts,
                         nrldpc_stream_t stream);
 
+/* ---- mixed-code batches (no reference counterpart; the reference compiles
+ * in one base graph and one Z per process, src/globals.h:15) ----------------
+ * A job is one codeword of any 5G NR (bg, z), optionally rate matched
+ * (3GPP TS 38.212 5.4.2.1 bit selection, full circular buffer, BPSK so no
+ * interleaver) with filler bits.  All offsets index caller buffers. */
+typedef struct {
+    int32_t bg, z;        /* base graph 1|2 and lifting size */
+    int32_t k_prime;      /* information bits before filler; 0 = kb*Z (no filler) */
+    int32_t e;            /* rate-matched length; 0 = one pass over the buffer */
+    int32_t rv;           /* redundancy version 0..3 */
+    float sigma;          /* noise std-dev (channel generator only) */
+    int64_t llr_offset;   /* float offset of the mother-code LLRs [cols*Z], multiple of 4 */
+    int64_t e_offset;     /* float offset of the rate-matched LLRs [e] */
+    int64_t out_offset;   /* byte offset of the packed hard decisions / codeword */
+} nrldpc_job;
+
+typedef struct nrldpc_batch nrldpc_batch;
+
+/* Tables of every (bg, z) on `device`, scratch for up to max_jobs jobs. */
+int nrldpc_batch_create(int device, int max_jobs, float alpha, nrldpc_batch** out);
+int nrldpc_batch_destroy(nrldpc_batch* b);
+/* Codewords per CTA for one code (the autotuner's knob); 0 restores the default. */
+int nrldpc_batch_set_cw_per_cta(nrldpc_batch* b, int bg, int z, int cw_per_cta);
+int nrldpc_batch_get_cw_per_cta(nrldpc_batch* b, int bg, int z, int* cw_per_cta);
+/* Load a job list (host array): validated, grouped by code into the device
+ * work queue (largest work first).  Synchronous. */
+int nrldpc_batch_set_jobs(nrldpc_batch* b, const nrldpc_job* jobs, int n_jobs);
+/* Seeded rate-matched transmissions of the loaded jobs (bit-identical to the
+ * oracle): d_llr_e at e_offset, transmitted codewords at out_offset of d_cw. */
+int nrldpc_batch_gen(nrldpc_batch* b, uint64_t seed, uint64_t cw_base, float* d_llr_e,
+                     uint8_t* d_cw, nrldpc_stream_t stream);
+/* De-rate-matching: rate-matched LLRs -> mother-code LLRs at llr_offset
+ * (punctured/unsent 0, filler +inf, repetitions added in order). */
+int nrldpc_batch_derate(nrldpc_batch* b, const float* d_llr_e, float* d_llr, nrldpc_stream_t stream);
+/* Decode all loaded jobs in one persistent launch (device work queue),
+ * replayed from a CUDA graph; d_iters (may be NULL) indexed by job. */
+int nrldpc_batch_decode(nrldpc_batch* b, const float* d_llr, uint8_t* d_packed, int n_iter,
+                        int early_stop, int32_t* d_iters, nrldpc_stream_t stream);
+/* d_counts[2] += {bit errors, frame errors} over each job's k_prime info bits. */
+int nrldpc_batch_count_errors(nrldpc_batch* b, const uint8_t* d_packed, const uint8_t* d_cw,
+                              unsigned long long* d_counts, nrldpc_stream_t stream);
+/* Host helper: k0 of redundancy version rv (TS 38.212 Table 5.4.2.1-2, full buffer). */
+int nrldpc_rm_k0(int bg, int z, int rv);
+
 /* Decode without allocating anything (no reference counterpart).  For
  * callers that cannot call cudaMalloc at decode time -- a physical-layer
  * pipeline that reserves all device memory at start-up and must not allocate
@@ -166,6 +210,14 @@ int nrldpc_count_errors(nrldpc_handle* h, const uint8_t* d_packed, const uint8_t
  * Calls share the array: calls that overlap on the GPU race; serialise them. */
 int nrldpc_decode_noalloc(int bg, int z, float alpha, const float* d_llr, uint8_t* d_packed,
                           int n_cw, int n_iter, int early_stop, nrldpc_stream_t stream);
+
+/* CRC (3GPP TS 38.212 5.1) of the first n_bits of each of n_cw packed
+ * words (stride_bytes apart); bit i of the packed bytes is the i-th bit of
+ * the sequence.  crc_type 0 = CRC24A, 1 = CRC24B, 2 = CRC16.  d_rem[i] = 0
+ * when the sequence ends in its own valid CRC.  No reference counterpart
+ * (the reference computes the CRC length only, src/nr_ldpc.cpp:37). */
+int nrldpc_crc(const uint8_t* d_packed, int n_cw, int stride_bytes, int n_bits, int crc_type,
+               uint32_t* d_rem, nrldpc_stream_t stream);
 
 /* Last device-side error recorded by a bounded wait (0 if none); clears it. */
 int nrldpc_device_error(nrldpc_handle* h);

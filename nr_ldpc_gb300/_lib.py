@@ -56,6 +56,17 @@ SIGNATURES = {
     "nrldpc_adam_step": (_i, [_i, _vp, _vp, _vp, _vp, _i, _f, _f, _f, _f, _f, _vp]),
     "nrldpc_gen_llr": (_i, [_vp, _u64, _u64, _i, _vp, _i, _vp, _vp, _vp]),
     "nrldpc_count_errors": (_i, [_vp, _vp, _vp, _i, _i, _vp, _vp]),
+    "nrldpc_batch_create": (_i, [_i, _i, _f, C.POINTER(_vp)]),
+    "nrldpc_batch_destroy": (_i, [_vp]),
+    "nrldpc_batch_set_cw_per_cta": (_i, [_vp, _i, _i, _i]),
+    "nrldpc_batch_get_cw_per_cta": (_i, [_vp, _i, _i, _ip]),
+    "nrldpc_batch_set_jobs": (_i, [_vp, _vp, _i]),
+    "nrldpc_batch_gen": (_i, [_vp, _u64, _u64, _vp, _vp, _vp]),
+    "nrldpc_batch_derate": (_i, [_vp, _vp, _vp, _vp]),
+    "nrldpc_batch_decode": (_i, [_vp, _vp, _vp, _i, _i, _vp, _vp]),
+    "nrldpc_batch_count_errors": (_i, [_vp, _vp, _vp, _vp, _vp]),
+    "nrldpc_rm_k0": (_i, [_i, _i, _i]),
+    "nrldpc_crc": (_i, [_vp, _i, _i, _i, _i, _vp, _vp]),
     "nrldpc_decode_noalloc": (_i, [_i, _i, _f, _vp, _vp, _i, _i, _i, _vp]),
     "nrldpc_device_error": (_i, [_vp]),
     "nrldpc_status_string": (C.c_char_p, [_i]),

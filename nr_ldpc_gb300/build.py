@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libnrldpc_gb300.so")
-SOURCES = ["decode.cu", "channel.cu", "wms.cu", "capi.cu", "noalloc.cu"]
+SOURCES = ["decode.cu", "channel.cu", "wms.cu", "batch.cu", "capi.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 

@@ -490,6 +490,21 @@ int nrldpc_count_errors(nrldpc_handle* handle, const uint8_t* d_packed, const ui
                                         d_counts, reinterpret_cast<cudaStream_t>(stream)));
 }
 
+int nrldpc_crc(const uint8_t* d_packed, int n_cw, int stride_bytes, int n_bits, int crc_type,
+               uint32_t* d_rem, nrldpc_stream_t stream) {
+    // generator polynomials of TS 38.212 5.1 without the leading term:
+    //   CRC24A: D^24+D^23+D^18+D^17+D^14+D^11+D^10+D^7+D^6+D^5+D^4+D^3+D+1
+    //   CRC24B: D^24+D^23+D^6+D^5+D+1          CRC16: D^16+D^12+D^5+1
+    static const uint32_t polys[3] = {0x864CFBu, 0x800063u, 0x1021u};
+    static const int lens[3] = {24, 24, 16};
+    if (crc_type < 0 || crc_type > 2 || n_cw < 0 || n_bits < 0 || stride_bytes * 8 < n_bits)
+        return NRLDPC_ERR_INVALID_ARG;
+    if (n_cw == 0) return NRLDPC_OK;
+    if (!d_packed || !d_rem) return NRLDPC_ERR_INVALID_ARG;
+    return map_cuda(launch_crc(d_packed, n_cw, stride_bytes, n_bits, polys[crc_type], lens[crc_type],
+                               d_rem, reinterpret_cast<cudaStream_t>(stream)));
+}
+
 int nrldpc_device_error(nrldpc_handle* handle) {
     Handle* h = reinterpret_cast<Handle*>(handle);
     if (!h) return NRLDPC_ERR_INVALID_ARG;

@@ -265,6 +265,65 @@ __device__ __forceinline__ uint32_t iterate_rows(const CodeTable& tab, uint32_t 
     return fail;
 }
 
+// Per-slot destinations of one decoded codeword (null pointers: not wanted).
+struct SlotOut {
+    uint8_t* packed;
+    float* app;
+    int32_t* iters;
+};
+
+// All iterations of one codeword group already loaded into buf0 (Lold):
+// cpb slots, this thread = sub-row s of slot `slot`.  Ends with a barrier.
+template <bool WEIGHTED>
+__device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slot, uint32_t s,
+                                          bool slot_done, float* buf0, float2* wpair, int* s_fail,
+                                          uint32_t* st_base, SlotOut out, int n_iter, int early_stop,
+                                          float alpha, const float* weights, int n_w_iters) {
+    const int z = tab.z, n = tab.n_bp, tid = threadIdx.x;
+    float* lold = buf0 + static_cast<size_t>(slot) * n;  // read by the check-node pass
+    float* lnew = lold + static_cast<size_t>(cpb) * n;   // accumulates the new posterior
+    const uint32_t s4old = smem_addr(lold) + 4u * s;
+    const uint32_t dnew = static_cast<uint32_t>(cpb) * static_cast<uint32_t>(n) * 4u;
+    if (!slot_done)
+        for (int k = static_cast<int>(s); k < n / 4; k += z)
+            reinterpret_cast<float4*>(lnew)[k] = reinterpret_cast<const float4*>(lold)[k];
+    for (int t = 0; t < n_iter; t++) {
+        const bool first = t == 0, last = t == n_iter - 1;
+        if (WEIGHTED) {
+            const int tp = min(max(t - 1, 0), n_w_iters - 1), tc = min(t, n_w_iters - 1);
+            for (int e = tid; e < tab.n_edges; e += blockDim.x)  // no previous R at t = 0
+                wpair[e] = make_float2(first ? 0.0f : weights[tp * tab.n_edges + e],
+                                       weights[tc * tab.n_edges + e]);
+        }
+        if (tid < cpb) s_fail[tid] = 0;
+        __syncthreads();
+        const bool act = !slot_done;
+        const bool check = early_stop && t > 0;
+        const uint32_t fail =
+            check ? iterate_rows<WEIGHTED, true>(tab, s, s4old, dnew, wpair, st_base, act, first, last,
+                                                alpha)
+                  : iterate_rows<WEIGHTED, false>(tab, s, s4old, dnew, wpair, st_base, act, first, last,
+                                                 alpha);
+        if (check) {
+            if (act && fail) atomicOr(&s_fail[slot], 1);
+            __syncthreads();
+            const bool conv = act && s_fail[slot] == 0;
+            if (conv)  // HD of the previous iteration is a codeword
+                write_outputs(tab, lold, s, out.packed, out.app, out.iters, t);
+            slot_done = slot_done || conv;
+            if (__syncthreads_and(slot_done)) break;
+        }
+        if (last) {
+            if (!slot_done) write_outputs(tab, lnew, s, out.packed, out.app, out.iters, n_iter);
+            break;
+        }
+        if (!slot_done)  // the posterior just accumulated is the next iteration's input
+            for (int k = static_cast<int>(s); k < n / 4; k += z)
+                reinterpret_cast<float4*>(lold)[k] = reinterpret_cast<const float4*>(lnew)[k];
+    }
+    __syncthreads();  // buffers are rewritten by the next group's copy
+}
+
 // MINB = CTAs per SM the register budget is sized for: 1 when shared memory
 // admits a single CTA per SM anyway (BG1 Z=384), 2 otherwise.
 template <bool WEIGHTED, int MINB>
@@ -276,15 +335,13 @@ __global__ void __launch_bounds__(kMaxThreads, MINB)
     int* s_fail = reinterpret_cast<int*>(smem + 16);
     float2* wpair = reinterpret_cast<float2*>(smem + kHeaderBytes);
     const int wbytes = WEIGHTED ? kMaxEdges * 8 : 0;
-    float* bufs = reinterpret_cast<float*>(smem + kHeaderBytes + wbytes);
+    float* buf0 = reinterpret_cast<float*>(smem + kHeaderBytes + wbytes);
 
     const int z = tab.z, n = tab.n_bp, cpb = a.cpb, rows = tab.rows;
     const int tid = threadIdx.x;
     const int slot = tid / z;
     const uint32_t s = static_cast<uint32_t>(tid - slot * z);
     const bool valid_thread = slot < cpb;
-    float* buf0 = bufs;
-    float* buf1 = bufs + static_cast<size_t>(cpb) * n;
     uint32_t* st_base =
         a.state + (static_cast<size_t>(blockIdx.x) * cpb + (valid_thread ? slot : 0)) * 3 * rows * z;
 
@@ -315,58 +372,73 @@ __global__ void __launch_bounds__(kMaxThreads, MINB)
             return;
         }
         phase ^= 1u;
+        const bool slot_done = !valid_thread || slot >= n_valid;
+        const size_t cw = static_cast<size_t>(cw0 + (slot_done ? 0 : slot));
+        SlotOut out{a.packed + cw * tab.packed_bytes, a.app ? a.app + cw * n : nullptr,
+                    a.iters ? a.iters + cw : nullptr};
+        run_group<WEIGHTED>(tab, cpb, slot, s, slot_done, buf0, wpair, s_fail, st_base, out, a.n_iter,
+                            a.early_stop, a.alpha, a.weights, a.n_w_iters);
+    }
+}
 
-        bool slot_done = !valid_thread || slot >= n_valid;
-        const int cw = cw0 + slot;
-        float* lold = buf0 + static_cast<size_t>(slot) * n;  // read by the check-node pass
-        float* lnew = buf1 + static_cast<size_t>(slot) * n;  // accumulates the new posterior
-        const uint32_t s4old = smem_addr(lold) + 4u * s;
-        const uint32_t dnew = static_cast<uint32_t>(cpb) * static_cast<uint32_t>(n) * 4u;
-        if (!slot_done)
-            for (int k = static_cast<int>(s); k < n / 4; k += z)
-                reinterpret_cast<float4*>(lnew)[k] = reinterpret_cast<const float4*>(lold)[k];
-        for (int t = 0; t < a.n_iter; t++) {
-            const bool first = t == 0, last = t == a.n_iter - 1;
-            if (WEIGHTED) {
-                const int nw = a.n_w_iters;
-                const int tp = min(max(t - 1, 0), nw - 1), tc = min(t, nw - 1);
-                for (int e = tid; e < tab.n_edges; e += blockDim.x)  // no previous R at t = 0
-                    wpair[e] = make_float2(first ? 0.0f : a.weights[tp * tab.n_edges + e],
-                                           a.weights[tc * tab.n_edges + e]);
-            }
-            if (tid < cpb) s_fail[tid] = 0;
-            __syncthreads();
-            const bool act = !slot_done;
-            const bool check = a.early_stop && t > 0;
-            const uint32_t fail =
-                check ? iterate_rows<WEIGHTED, true>(tab, s, s4old, dnew, wpair, st_base, act, first,
-                                                    last, a.alpha)
-                      : iterate_rows<WEIGHTED, false>(tab, s, s4old, dnew, wpair, st_base, act, first,
-                                                     last, a.alpha);
-            if (check) {
-                if (act && fail) atomicOr(&s_fail[slot], 1);
-                __syncthreads();
-                const bool conv = act && s_fail[slot] == 0;
-                if (conv && cw < a.n_cw) {  // HD of the previous iteration is a codeword
-                    write_outputs(tab, lold, s, a.packed + static_cast<size_t>(cw) * tab.packed_bytes,
-                                  a.app ? a.app + static_cast<size_t>(cw) * n : nullptr,
-                                  a.iters ? a.iters + cw : nullptr, t);
-                }
-                slot_done = slot_done || conv;
-                if (__syncthreads_and(slot_done)) break;
-            }
-            if (last) {
-                if (!slot_done)
-                    write_outputs(tab, lnew, s, a.packed + static_cast<size_t>(cw) * tab.packed_bytes,
-                                  a.app ? a.app + static_cast<size_t>(cw) * n : nullptr,
-                                  a.iters ? a.iters + cw : nullptr, a.n_iter);
-                break;
-            }
-            if (!slot_done)  // the posterior just accumulated is the next iteration's input
-                for (int k = static_cast<int>(s); k < n / 4; k += z)
-                    reinterpret_cast<float4*>(lold)[k] = reinterpret_cast<const float4*>(lnew)[k];
+// Mixed batch: one persistent launch over work items of several (BG, Z)
+// codes.  Each item = up to cpb codewords of one code; the item's code table
+// is copied into shared memory and every codeword is fetched from its own
+// offset with its own bulk copy.
+__global__ void __launch_bounds__(kMaxThreads, 1)
+    batch_decode_kernel(const __grid_constant__ BatchDecodeArgs a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const uint32_t bar = smem_addr(smem);
+    int* s_item = reinterpret_cast<int*>(smem + 8);
+    int* s_fail = reinterpret_cast<int*>(smem + 16);
+    CodeTable* stab = reinterpret_cast<CodeTable*>(smem + kHeaderBytesBatch);
+    float* buf0 = reinterpret_cast<float*>(smem + kHeaderBytesBatch + kBatchTableBytes);
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    for (;;) {
+        if (tid == 0) *s_item = atomicAdd(a.work_counter, 1);
+        __syncthreads();
+        const int it = *s_item;
+        if (it >= a.n_items) break;
+        const WorkItem item = a.items[it];
+        {   // code table of this item into shared memory
+            const uint4* src = reinterpret_cast<const uint4*>(a.tables + item.code);
+            uint4* dst = reinterpret_cast<uint4*>(stab);
+            for (int k = tid; k < static_cast<int>(sizeof(CodeTable) / 16); k += blockDim.x) dst[k] = src[k];
         }
-        __syncthreads();  // buffers are rewritten by the next group's copy
+        __syncthreads();
+        const CodeTable& tab = *stab;
+        const int z = tab.z, n = tab.n_bp, cpb = item.count;
+        const int slot = tid / z;
+        const uint32_t s = static_cast<uint32_t>(tid - slot * z);
+        const bool valid_thread = slot < cpb;
+        if (tid == 0) {
+            fence_proxy_async();
+            mbar_arrive_expect_tx(bar, static_cast<uint32_t>(cpb) * n * 4u);
+            for (int k = 0; k < cpb; k++) {
+                const nrldpc_job& j = a.jobs[a.order[item.start + k]];
+                bulk_g2s(smem_addr(buf0 + static_cast<size_t>(k) * n), a.llr + j.llr_offset, n * 4u, bar);
+            }
+        }
+        bool ok = mbar_wait_bounded(bar, phase);
+        if (!__syncthreads_and(ok)) {
+            if (tid == 0) atomicExch(a.error_flag, kErrLlrLoadTimeout);
+            mbar_wait_bounded(bar, phase);
+            return;
+        }
+        phase ^= 1u;
+        const int jidx = valid_thread ? a.order[item.start + slot] : 0;
+        const nrldpc_job& job = a.jobs[jidx];
+        SlotOut out{a.packed + job.out_offset, nullptr, a.iters ? a.iters + jidx : nullptr};
+        uint32_t* st_base = a.state + static_cast<size_t>(blockIdx.x) * a.slot_words +
+                            static_cast<size_t>(valid_thread ? slot : 0) * 3 * tab.rows * z;
+        run_group<false>(tab, cpb, slot, s, !valid_thread, buf0, nullptr, s_fail, st_base, out, a.n_iter,
+                         a.early_stop, a.alpha, nullptr, 1);
     }
 }
 
@@ -387,7 +459,18 @@ const void* select_kernel(bool weighted, int minb) {
     return minb >= 2 ? kernel_ptr<false, 2>() : kernel_ptr<false, 1>();
 }
 
+cudaError_t launch_batch_decode(const BatchDecodeArgs& args, int grid, size_t smem, cudaStream_t stream) {
+    batch_decode_kernel<<<grid, kMaxThreads, smem, stream>>>(args);
+    return cudaGetLastError();
+}
+
+const void* batch_decode_kernel_ptr() { return reinterpret_cast<const void*>(&batch_decode_kernel); }
+
 cudaError_t decode_kernel_attributes(size_t smem) {
+    cudaError_t e = cudaFuncSetAttribute(batch_decode_kernel_ptr(),
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
     for (int w = 0; w < 2; w++)
         for (int m = 1; m <= 2; m++) {
             cudaError_t e = cudaFuncSetAttribute(select_kernel(w != 0, m),

@@ -5,6 +5,8 @@
 #include <cstddef>
 #include <cstdint>
 
+#include "../../include/nr_ldpc_gb300.h"
+
 namespace nrldpc {
 
 constexpr int kMaxRows = 46;    // BG1
@@ -15,7 +17,7 @@ constexpr int kMaxZ = 384;
 constexpr int kMaxThreads = 384;  // decode CTA size bound (cw_per_cta * Z)
 
 // Lifted-code description passed to kernels by value (__grid_constant__).
-struct CodeTable {
+struct alignas(16) CodeTable {
     int rows, cols, z, n_edges, n_bp, packed_bytes;
     int kb;                        // systematic base columns (encoder)
     uint16_t row_ptr[kMaxRows + 1];
@@ -53,6 +55,34 @@ struct DecodeArgs {
 
 enum DeviceError : int { kErrNone = 0, kErrLlrLoadTimeout = 1 };
 
+// Mixed-code batches (batch.cu): a work item is up to `count` codewords of
+// one code, listed at order[start .. start+count).
+struct WorkItem {
+    int32_t code;   // index into the table array
+    int32_t start;
+    int32_t count;
+    int32_t pad;
+};
+constexpr size_t kHeaderBytesBatch = 1024;  // mbarrier, item id, per-slot flags
+constexpr size_t kBatchTableBytes = (sizeof(CodeTable) + 127) / 128 * 128;
+struct BatchDecodeArgs {
+    const CodeTable* tables;
+    const WorkItem* items;
+    const int32_t* order;       // job indices sorted by code
+    const nrldpc_job* jobs;
+    const float* llr;
+    uint8_t* packed;
+    int32_t* iters;
+    uint32_t* state;            // [grid][slot_words]
+    int* work_counter;
+    int* error_flag;
+    size_t slot_words;          // state words per CTA (largest cpb * 3 * rows * Z)
+    int n_items, n_iter, early_stop;
+    float alpha;
+};
+cudaError_t launch_batch_decode(const BatchDecodeArgs& args, int grid, size_t smem, cudaStream_t stream);
+const void* batch_decode_kernel_ptr();
+
 // Host-side launchers (decode.cu / channel.cu).
 // minb: CTAs per SM the kernel's register budget assumes (1 or 2).
 cudaError_t launch_decode(const CodeTable& tab, const DecodeArgs& args, int grid, int threads,
@@ -85,6 +115,8 @@ bool make_encode_plan(const CodeTable& tab, EncodePlan* plan);
 cudaError_t launch_gen_llr(const CodeTable& tab, const EncodePlan& plan, uint64_t seed,
                            uint64_t cw_base, int n_cw, const float* sigma, int n_punct_cols,
                            float* llr, uint8_t* cw_packed, cudaStream_t stream);
+cudaError_t launch_crc(const uint8_t* packed, int n_cw, int stride, int n_bits, uint32_t poly, int len,
+                       uint32_t* rem, cudaStream_t stream);
 cudaError_t launch_count_errors(const uint8_t* packed, const uint8_t* cw_packed, int n_cw,
                                 int packed_bytes, int n_info, unsigned long long* counts,
                                 cudaStream_t stream);

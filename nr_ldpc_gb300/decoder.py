@@ -38,6 +38,9 @@ class Decoder:
     def __init__(self, bg: int = 1, z: int = 384, max_batch: int = 4096, alpha: float = 0.75,
                  device: int = 0, cw_per_cta: int = 0, base: Optional[np.ndarray] = None):
         lib = _lib.load()
+        if cw_per_cta == 0 and base is None:
+            from .autotune import load_table
+            cw_per_cta = load_table(device).get((bg, z), 0)
         cfg = _lib.ConfigC(bg=bg if base is None else 0, z=z, max_batch=max_batch, alpha=alpha,
                            device=device, cw_per_cta=cw_per_cta)
         h = C.c_void_p()

@@ -503,6 +503,119 @@ int orc_gen_llr(const orc_code* c, int kb, uint64_t seed, uint64_t cw_base, int 
 }
 
 /* ------------------------------------------------------------------------- */
+/* Rate matching, TS 38.212 5.4.2.1 (full circular buffer, BPSK).            */
+int orc_rm_k0(int bg, int z, int rv) {
+    /* k0 = floor(a * Ncb / (n * Z)) * Z with Ncb = n * Z: a per BG and rv */
+    static const int a1[4] = {0, 17, 33, 56}, a2[4] = {0, 13, 25, 43};
+    if (rv < 0 || rv > 3 || (bg != 1 && bg != 2)) return -1;
+    const int n = bg == 1 ? 66 : 50;
+    const long ncb = (long)n * z;
+    return (int)(((bg == 1 ? a1[rv] : a2[rv]) * ncb) / ((long)n * z)) * z;
+}
+
+/* Non-NULL positions form a compressed buffer of Ncb - F entries; bit k is
+ * compressed entry (c0 + k) mod (Ncb - F), c0 = k0 with the filler run
+ * [f0, f1) of d removed (a k0 inside the run starts right after it). */
+int orc_rm_index(int z, int ncb, int kb_z, int k_prime, int k0, int k) {
+    const int f0 = k_prime - 2 * z, f1 = kb_z - 2 * z, nf = f1 - f0, nc = ncb - nf;
+    const int c0 = k0 < f0 ? k0 : (k0 < f1 ? f0 : k0 - nf);
+    const int c = (int)(((long)c0 + k) % nc);
+    return c < f0 ? c : c + nf;
+}
+
+int orc_gen_rm_llr(const orc_code* c, int kb, int bg, uint64_t seed, uint64_t cw_base, int n_cw,
+                   const float* sigma, const int* k_prime, const int* e, const int* rv,
+                   int e_stride, float* llr_e, uint8_t* cw_packed) {
+    const int z = c->z, N = c->cols * z, K = kb * z, ncb = N - 2 * z;
+    const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    uint8_t* info = (uint8_t*)malloc(K);
+    uint8_t* cwp = (uint8_t*)malloc(PACKED_BYTES(N));
+    int rc = 0;
+    for (int i = 0; i < n_cw && !rc; i++) {
+        const uint64_t id = cw_base + (uint64_t)i;
+        const int kp = k_prime[i] > 0 ? k_prime[i] : K;
+        if (kp > K || kp < 2 * z || e[i] > e_stride || e[i] < 1) { rc = -1; break; }
+        for (int blk = 0; blk * 128 < K; blk++) {
+            uint32_t ctr[4] = {(uint32_t)blk, (uint32_t)id, (uint32_t)(id >> 32), 1u}, o[4];
+            orc_philox4x32(ctr, key, o);
+            for (int b = 0; b < 128 && blk * 128 + b < K; b++) {
+                const int pos = blk * 128 + b;
+                info[pos] = pos < kp ? (o[b >> 5] >> (b & 31)) & 1 : 0;
+            }
+        }
+        rc = orc_encode(c, kb, info, cwp);
+        if (rc) break;
+        if (cw_packed) memcpy(cw_packed + (size_t)i * PACKED_BYTES(N), cwp, PACKED_BYTES(N));
+        const int k0 = orc_rm_k0(bg, z, rv[i]);
+        const float sg = sigma[i], s2 = sg * sg;
+        float* out = llr_e + (size_t)i * e_stride;
+        for (int t = 0; t * 4 < e[i]; t++) {
+            uint32_t ctr[4] = {(uint32_t)t, (uint32_t)id, (uint32_t)(id >> 32), 3u}, o[4];
+            orc_philox4x32(ctr, key, o);
+            float g[4];
+            for (int h = 0; h < 2; h++) {
+                const float u1 = u01_open0(o[2 * h]), u2 = u01_open1(o[2 * h + 1]);
+                float l = orc_logf(u1);
+                l = l * -2.0f;
+                const float rad = sqrtf(l);
+                float sn, cs;
+                orc_sincos2pi(u2, &sn, &cs);
+                g[2 * h] = rad * cs;
+                g[2 * h + 1] = rad * sn;
+            }
+            for (int q = 0; q < 4 && 4 * t + q < e[i]; q++) {
+                const int k = 4 * t + q;
+                const int j = 2 * z + orc_rm_index(z, ncb, K, kp, k0, k);
+                const int bit = (cwp[j >> 3] >> (j & 7)) & 1;
+                const float x = bit ? -1.0f : 1.0f;
+                const float ns = g[q] * sg;
+                const float y = x + ns;
+                const float y2 = y * 2.0f;
+                out[k] = y2 / s2;
+            }
+        }
+    }
+    free(info); free(cwp);
+    return rc;
+}
+
+int orc_derate_match(const orc_code* c, int kb, int bg, int n_cw, const float* llr_e, int e_stride,
+                     const int* k_prime, const int* e, const int* rv, float* llr) {
+    const int z = c->z, N = c->cols * z, K = kb * z, ncb = N - 2 * z;
+    uint8_t* seen = (uint8_t*)malloc(N);
+    for (int i = 0; i < n_cw; i++) {
+        const int kp = k_prime[i] > 0 ? k_prime[i] : K;
+        if (kp > K || kp < 2 * z || e[i] > e_stride || e[i] < 1) { free(seen); return -1; }
+        const int k0 = orc_rm_k0(bg, z, rv[i]);
+        float* out = llr + (size_t)i * N;
+        for (int j = 0; j < N; j++) out[j] = 0.0f;
+        for (int j = kp; j < K; j++) out[j] = INFINITY; /* filler: known 0 */
+        memset(seen, 0, N);
+        for (int k = 0; k < e[i]; k++) {
+            const int j = 2 * z + orc_rm_index(z, ncb, K, kp, k0, k);
+            const float v = llr_e[(size_t)i * e_stride + k];
+            if (seen[j]) out[j] = out[j] + v;
+            else { out[j] = v; seen[j] = 1; }
+        }
+    }
+    free(seen);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+uint32_t orc_crc(const uint8_t* packed, int n_bits, uint32_t poly, int len) {
+    const uint32_t top = 1u << (len - 1), mask = (len == 32) ? 0xffffffffu : ((1u << len) - 1u);
+    uint32_t r = 0;
+    for (int i = 0; i < n_bits; i++) {
+        const uint32_t bit = (packed[i >> 3] >> (i & 7)) & 1u;
+        const uint32_t fb = ((r & top) != 0) ^ bit;
+        r = (r << 1) & mask;
+        if (fb) r ^= poly;
+    }
+    return r;
+}
+
+/* ------------------------------------------------------------------------- */
 /* Learned weighted min-sum: forward + adjoint in double precision.          */
 static inline double softplus(double x) { return x > 0 ? x + log1p(exp(-x)) : log1p(exp(x)); }
 static inline double sigm(double x) { return x >= 0 ? 1.0 / (1.0 + exp(-x)) : exp(x) / (1.0 + exp(x)); }

@@ -68,6 +68,33 @@ int orc_encode(const orc_code* c, int kb, const uint8_t* info, uint8_t* cw_packe
 int orc_gen_llr(const orc_code* c, int kb, uint64_t seed, uint64_t cw_base, int n_cw,
                 const float* sigma, int n_punct_cols, float* llr, uint8_t* cw_packed);
 
+/* ---- rate matching (no reference counterpart; 3GPP TS 38.212 5.4.2.1) ------
+ * Mother codeword x[cols*Z]; circular buffer d[j] = x[2Z + j], Ncb = cols*Z - 2Z
+ * (full buffer); filler bits x[k_prime .. kb*Z) are NULL (never sent, known 0).
+ * k0 from rv as the standard's table; E bits e_k = d[(k0 + j) mod Ncb] taken in
+ * order skipping NULLs.  BPSK, so no bit interleaving. */
+int orc_rm_k0(int bg, int z, int rv);
+/* d index (0 .. Ncb-1) of rate-matched bit k. */
+int orc_rm_index(int z, int ncb, int kb_z, int k_prime, int k0, int k);
+/* Seeded rate-matched transmission: info bits (k_prime random, filler 0),
+ * encode, select e bits, BPSK + AWGN sigma[i]; llr_e [n_cw][e_stride]. */
+int orc_gen_rm_llr(const orc_code* c, int kb, int bg, uint64_t seed, uint64_t cw_base, int n_cw,
+                   const float* sigma, const int* k_prime, const int* e, const int* rv,
+                   int e_stride, float* llr_e, uint8_t* cw_packed);
+/* Receiver: rate-matched LLRs -> mother-code LLRs [n_cw][cols*Z]: punctured
+ * and unsent columns 0, filler +inf, repeated bits added in transmission
+ * order (first copy taken as is). */
+int orc_derate_match(const orc_code* c, int kb, int bg, int n_cw, const float* llr_e, int e_stride,
+                     const int* k_prime, const int* e, const int* rv, float* llr);
+
+/* ---- CRC (3GPP TS 38.212 5.1), bitwise long division ------------------------
+ * poly: generator without the leading term (CRC24A 0x864CFB, CRC24B 0x800063,
+ * CRC16 0x1021), len = 24 or 16.  Bits a_0 .. a_{n-1} are bit i of the packed
+ * bytes (LSB first); a_0 is the highest-order coefficient.  Returns the
+ * remainder of a(D) * D^len; appending its bits p_0..p_{len-1} (p_0 = MSB)
+ * gives a sequence whose remainder over n+len bits is 0. */
+uint32_t orc_crc(const uint8_t* packed, int n_bits, uint32_t poly, int len);
+
 /* Philox4x32-10 block (Salmon et al., SC'11) and the float helpers used by the
  * generator, exposed for the generator's own tests. */
 void orc_philox4x32(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);

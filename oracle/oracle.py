@@ -61,6 +61,14 @@ def lib():
                                             C.c_void_p, C.c_void_p]
         L.orc_wms_decode_f32.argtypes = [C.c_void_p, _f32p, C.c_int, C.c_int, _f32p, C.c_int,
                                          C.c_int, _u8p, C.c_void_p, C.c_void_p]
+        L.orc_crc.restype = C.c_uint32
+        L.orc_crc.argtypes = [_u8p, C.c_int, C.c_uint32, C.c_int]
+        L.orc_rm_k0.argtypes = [C.c_int, C.c_int, C.c_int]
+        L.orc_rm_index.argtypes = [C.c_int] * 6
+        L.orc_gen_rm_llr.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_uint64, C.c_uint64, C.c_int,
+                                     _f32p, _i32p, _i32p, _i32p, C.c_int, _f32p, C.c_void_p]
+        L.orc_derate_match.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _f32p, C.c_int,
+                                       _i32p, _i32p, _i32p, _f32p]
         _lib = L
     return _lib
 
@@ -156,6 +164,50 @@ class OracleCode:
         if rc:
             raise RuntimeError(f"orc_wms_decode_f32 rc={rc}")
         return packed, app, iters
+
+
+CRC24A, CRC24B, CRC16 = (0x864CFB, 24), (0x800063, 24), (0x1021, 16)
+
+
+def crc(packed, n_bits, poly_len):
+    return lib().orc_crc(np.ascontiguousarray(packed, np.uint8), int(n_bits), poly_len[0], poly_len[1])
+
+
+def rm_k0(bg, z, rv):
+    return lib().orc_rm_k0(bg, z, rv)
+
+
+def rm_index(z, ncb, kb_z, k_prime, k0, k):
+    return lib().orc_rm_index(z, ncb, kb_z, k_prime, k0, k)
+
+
+def gen_rm_llr(oc, kb, bg, seed, cw_base, sigma, k_prime, e, rv):
+    sigma = np.ascontiguousarray(np.atleast_1d(sigma), np.float32)
+    n = sigma.shape[0]
+    kp = np.ascontiguousarray(np.broadcast_to(k_prime, (n,)), np.int32)
+    ee = np.ascontiguousarray(np.broadcast_to(e, (n,)), np.int32)
+    rr = np.ascontiguousarray(np.broadcast_to(rv, (n,)), np.int32)
+    stride = int(ee.max())
+    llr_e = np.zeros((n, stride), np.float32)
+    cw = np.zeros((n, oc.n_bytes), np.uint8)
+    rc = lib().orc_gen_rm_llr(oc._h, kb, bg, int(seed), int(cw_base), n, sigma, kp, ee, rr, stride,
+                              llr_e, _ptr(cw))
+    if rc:
+        raise RuntimeError(f"orc_gen_rm_llr rc={rc}")
+    return llr_e, cw
+
+
+def derate_match(oc, kb, bg, llr_e, k_prime, e, rv):
+    llr_e = np.ascontiguousarray(llr_e, np.float32)
+    n, stride = llr_e.shape
+    kp = np.ascontiguousarray(np.broadcast_to(k_prime, (n,)), np.int32)
+    ee = np.ascontiguousarray(np.broadcast_to(e, (n,)), np.int32)
+    rr = np.ascontiguousarray(np.broadcast_to(rv, (n,)), np.int32)
+    out = np.zeros((n, oc.n_bp), np.float32)
+    rc = lib().orc_derate_match(oc._h, kb, bg, n, llr_e, stride, kp, ee, rr, out)
+    if rc:
+        raise RuntimeError(f"orc_derate_match rc={rc}")
+    return out
 
 
 def philox4x32(ctr, key):
