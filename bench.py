@@ -30,7 +30,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "info Gbit/s at FER<=1e-2 (BG1 Z=384 normalized min-sum, 10 iterations)"
+METRIC = "info Gbit/s at FER\u22641e-2: learned weighted vs plain min-sum, same GB300"
 BG, Z, ITERS, BATCH, EBN0 = 1, 384, 10, 4096, 2.0
 K_INFO, N_BP, E_EDGES = 8448, 26112, 316
 
@@ -156,6 +156,55 @@ def run_e2e(dec, llr, packed, steps, stream, world):
     return e2e_ms
 
 
+def learned_vs_plain(dec, stream, batch: int, ebn0: float = 1.75, weights: str = "bg1_T10",
+                     frames: int = 32768, timed_steps: int = 10):
+    """Both decoders at one Eb/N0, early stop on: the smallest iteration cap
+    whose FER over `frames` fresh codewords is <= 1e-2, then info Gbit/s of
+    that configuration (LLRs resident, CUDA events).  Iterations past the
+    trained ones reuse the last weight row."""
+    import torch
+    from nr_ldpc_gb300 import codes
+    from nr_ldpc_gb300.learned import load_weights
+    sigma = codes.noise_sigma(ebn0, K_INFO / (N_BP - 2 * Z))
+    sig = torch.full((batch,), sigma, dtype=torch.float32, device="cuda")
+    sets = [dec.gen_llr(seed=31, cw_base=(1 << 40) + k * batch, sigma=sig) for k in range(frames // batch)]
+    dec.set_weights(load_weights(weights))
+    out = torch.empty((batch, dec.packed_bytes), dtype=torch.uint8, device="cuda")
+    res = {}
+    for name, weighted, caps in (("plain", False, (10, 11, 12, 13, 14, 16, 18, 20)),
+                                 ("learned", True, (8, 9, 10, 11, 12, 14, 16, 18, 20))):
+        for cap in caps:
+            counts = torch.zeros(2, dtype=torch.int64, device="cuda")
+            its = torch.zeros(1, dtype=torch.int64, device="cuda")
+            for llr, cw in sets:
+                pk, it = dec.decode(llr, cap, early_stop=True, weighted=weighted, want_iters=True, out=out)
+                dec.count_errors(pk, cw, counts=counts)
+                its += it.sum()
+            torch.cuda.synchronize()
+            fer = int(counts[1]) / (len(sets) * batch)
+            if fer <= 1e-2 or cap == caps[-1]:
+                break
+        llr, _ = sets[0]
+        for _ in range(3):
+            dec.decode(llr, cap, early_stop=True, weighted=weighted, out=out)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(timed_steps):
+            dec.decode(llr, cap, early_stop=True, weighted=weighted, out=out, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / timed_steps
+        res[name] = {"iters_max": cap, "fer": fer, "frames": len(sets) * batch,
+                     "avg_iters": float(its.item()) / (len(sets) * batch),
+                     "info_gbps": batch * K_INFO / (ms * 1e-3) / 1e9, "ms_per_batch": ms}
+    res["learned"]["weights"] = weights
+    res["plain"]["alpha"] = 0.75
+    res["ebn0_db"] = ebn0
+    res["early_stop"] = True
+    res["speedup"] = res["learned"]["info_gbps"] / res["plain"]["info_gbps"]
+    return res, 1 + 2 * timed_steps + 6
+
+
 def cpu_baseline(llr_host: np.ndarray, n_sample: int):
     """Reference algorithm on the host cores: the oracle's C restatement of
     the reference min-sum (kind 'port'), all cores, one codeword per thread."""
@@ -222,6 +271,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling)")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain comparison")
     ap.add_argument("--batch", type=int, default=BATCH,
                     help="codewords per step (profiling a smaller launch; default 4096)")
     args = ap.parse_args()
@@ -280,6 +330,8 @@ def main():
     if not args.no_e2e:
         e2e_ms = run_e2e(dec, llr, packed, args.steps, stream, world)
 
+    lvp, lvp_launches = (None, 0) if args.no_learned else learned_vs_plain(dec, stream, min(B, 4096))
+
     peak, peak_kind = measured_peaks()
     bytes_launch = model_bytes_per_cw(ITERS) * B
     achieved = bytes_launch / (ms_launch * 1e-3) / 1e9
@@ -306,6 +358,8 @@ def main():
         "clocks": clocks,
         "gpu_launches": args.steps,
     }
+    if lvp is not None:
+        line["learned_vs_plain"] = lvp
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(llr.cpu().numpy(), n_sample=min(B, 1024))
     if rank == 0:

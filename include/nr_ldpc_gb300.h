@@ -109,6 +109,15 @@ int nrldpc_decode(nrldpc_handle* h, const float* d_llr, uint8_t* d_packed, int n
 int nrldpc_decode_host_async(nrldpc_handle* h, const float* h_llr, uint8_t* h_packed, int n_cw,
                              int n_iter, int early_stop, nrldpc_stream_t stream);
 
+/* As nrldpc_decode_host_async with narrow LLRs over the host link (the
+ * reference's CHAR_PRC / HALF_PRC transfer idea, src/setup_exp.cu:26-46,
+ * README TODO "make the memory transfer take place in fp16"): qtype 1 =
+ * IEEE fp16, 2 = int8 with LLR = q * scale.  Widened to fp32 on the GPU and
+ * decoded in fp32 (results = fp32 decode of the widened values). */
+int nrldpc_decode_host_async_q(nrldpc_handle* h, const void* h_llr_q, int qtype, float scale,
+                               uint8_t* h_packed, int n_cw, int n_iter, int early_stop,
+                               nrldpc_stream_t stream);
+
 /* Learned weighted min-sum: per (iteration, base edge) scale factors
  * w[n_w_iters][n_edges] replacing alpha (iterations past n_w_iters reuse the
  * last row).  Host pointer; copied into the handle.  n_w_iters = 0 clears. */

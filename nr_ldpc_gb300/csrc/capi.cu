@@ -33,6 +33,7 @@ struct Handle {
     int* scratch = nullptr;  // [0] work counter, [1] error flag
     float* stage_llr = nullptr;
     uint8_t* stage_packed = nullptr;
+    void* stage_q = nullptr;  // fp16 / int8 LLR staging (nrldpc_decode_host_async_q)
     float* weights = nullptr;
     int n_w_iters = 0;
     bool wms_ready = false;
@@ -112,6 +113,7 @@ void free_handle(Handle* h) {
     cudaFree(h->scratch);
     cudaFree(h->stage_llr);
     cudaFree(h->stage_packed);
+    cudaFree(h->stage_q);
     cudaFree(h->weights);
     delete h;
 }
@@ -374,6 +376,37 @@ int nrldpc_decode_host_async(nrldpc_handle* handle, const float* h_llr, uint8_t*
                                nullptr, false, s);
     if (rc) return rc;
     return map_cuda(cudaMemcpyAsync(h_packed, h->stage_packed, out_bytes, cudaMemcpyDeviceToHost, s));
+}
+
+int nrldpc_decode_host_async_q(nrldpc_handle* handle, const void* h_llr_q, int qtype, float scale,
+                               uint8_t* h_packed, int n_cw, int n_iter, int early_stop,
+                               nrldpc_stream_t stream) {
+    Handle* h = reinterpret_cast<Handle*>(handle);
+    if (!h || n_cw < 0 || (qtype != 1 && qtype != 2) || (qtype == 2 && !(scale > 0.0f)))
+        return NRLDPC_ERR_INVALID_ARG;
+    if (n_cw > h->max_batch) return NRLDPC_ERR_TOO_LARGE;
+    if (n_cw == 0) return NRLDPC_OK;
+    if (!h_llr_q || !h_packed) return NRLDPC_ERR_INVALID_ARG;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const size_t n = static_cast<size_t>(n_cw) * h->tab.n_bp;
+    const size_t qbytes = n * (qtype == 1 ? 2 : 1);
+    if (!h->stage_q) {  // narrow staging, allocated on the first call of this entry point
+        const size_t cap = static_cast<size_t>(h->max_batch) * h->tab.n_bp * 2;
+        if (cudaMalloc(&h->stage_q, cap) != cudaSuccess) {
+            h->stage_q = nullptr;
+            return NRLDPC_ERR_NO_MEMORY;
+        }
+    }
+    void* narrow = h->stage_q;
+    if (cudaMemcpyAsync(narrow, h_llr_q, qbytes, cudaMemcpyHostToDevice, s) != cudaSuccess)
+        return NRLDPC_ERR_CUDA;
+    if (launch_dequant(narrow, qtype, scale, n, h->stage_llr, s) != cudaSuccess) return NRLDPC_ERR_CUDA;
+    const int rc = decode_impl(h, h->stage_llr, h->stage_packed, n_cw, n_iter, early_stop, nullptr,
+                               nullptr, false, s);
+    if (rc) return rc;
+    return map_cuda(cudaMemcpyAsync(h_packed, h->stage_packed,
+                                    static_cast<size_t>(n_cw) * h->tab.packed_bytes,
+                                    cudaMemcpyDeviceToHost, s));
 }
 
 int nrldpc_set_weights(nrldpc_handle* handle, const float* w, int n_w_iters) {

@@ -11,6 +11,7 @@
 // evaluated from +, -, *, / and sqrt only.  Every float operation is an
 // explicit round-to-nearest intrinsic in the same order as the CPU oracle's
 // C code, so both produce the same bits.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <vector>
@@ -141,7 +142,28 @@ __global__ void __launch_bounds__(256) crc_kernel(const uint8_t* __restrict__ pa
     rem[cw] = r;
 }
 
+// Widen transferred LLRs to fp32: qtype 1 = IEEE half (exact), 2 = int8
+// times `scale` (one rounding, the product).
+__global__ void __launch_bounds__(256) dequant_kernel(const void* __restrict__ in, int qtype,
+                                                      float scale, size_t n, float* __restrict__ out) {
+    for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<size_t>(gridDim.x) * blockDim.x) {
+        if (qtype == 1)
+            out[i] = __half2float(__ushort_as_half(static_cast<const unsigned short*>(in)[i]));
+        else
+            out[i] = __fmul_rn(static_cast<float>(static_cast<const int8_t*>(in)[i]), scale);
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_dequant(const void* in, int qtype, float scale, size_t n, float* out,
+                           cudaStream_t stream) {
+    const size_t blocks = (n + 255) / 256;
+    dequant_kernel<<<static_cast<unsigned>(blocks < 4096 ? blocks : 4096), 256, 0, stream>>>(in, qtype, scale,
+                                                                                             n, out);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_crc(const uint8_t* packed, int n_cw, int stride, int n_bits, uint32_t poly, int len,
                        uint32_t* rem, cudaStream_t stream) {

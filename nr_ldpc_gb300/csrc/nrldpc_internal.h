@@ -115,6 +115,8 @@ bool make_encode_plan(const CodeTable& tab, EncodePlan* plan);
 cudaError_t launch_gen_llr(const CodeTable& tab, const EncodePlan& plan, uint64_t seed,
                            uint64_t cw_base, int n_cw, const float* sigma, int n_punct_cols,
                            float* llr, uint8_t* cw_packed, cudaStream_t stream);
+cudaError_t launch_dequant(const void* in, int qtype, float scale, size_t n, float* out,
+                           cudaStream_t stream);
 cudaError_t launch_crc(const uint8_t* packed, int n_cw, int stride, int n_bits, uint32_t poly, int len,
                        uint32_t* rem, cudaStream_t stream);
 cudaError_t launch_count_errors(const uint8_t* packed, const uint8_t* cw_packed, int n_cw,

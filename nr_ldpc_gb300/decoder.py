@@ -116,6 +116,23 @@ class Decoder:
                                                       int(n_iter), int(bool(early_stop)),
                                                       _stream_ptr(stream)))
 
+    def decode_host_q(self, llr_q_host: torch.Tensor, packed_host: torch.Tensor, n_iter: int,
+                      scale: float = 1.0, early_stop: bool = False,
+                      stream: Optional[torch.cuda.Stream] = None):
+        """Host call with fp16 (torch.float16) or int8 (LLR = q * scale) LLRs."""
+        if llr_q_host.dtype == torch.float16:
+            qtype = 1
+        elif llr_q_host.dtype == torch.int8:
+            qtype = 2
+        else:
+            raise ValueError("fp16 or int8 LLRs expected")
+        n = llr_q_host.numel() // self.n_bp
+        _lib.check("nrldpc_decode_host_async_q",
+                   self._lib.nrldpc_decode_host_async_q(self._h, C.c_void_p(llr_q_host.data_ptr()), qtype,
+                                                        float(scale), C.c_void_p(packed_host.data_ptr()),
+                                                        n, int(n_iter), int(bool(early_stop)),
+                                                        _stream_ptr(stream)))
+
     # ---- learned weights ------------------------------------------------------------
     def set_weights(self, w) -> None:
         w = np.ascontiguousarray(np.asarray(w, dtype=np.float32).reshape(-1, self.n_edges))

@@ -200,3 +200,26 @@ def test_count_errors_against_numpy(gpu):
     torch.cuda.synchronize()
     diff = np.unpackbits(a ^ b, axis=1, bitorder="little")[:, :77].sum(1)
     assert counts.tolist() == [int(diff.sum()), int((diff > 0).sum())]
+
+
+@pytest.mark.parametrize("qtype", ["f16", "i8"])
+def test_reduced_precision_host_transfer(gpu, qtype):
+    """fp16 / int8 LLRs over the host link decode exactly like the fp32
+    decode of the widened values (the oracle on the same values)."""
+    dec = Decoder(bg=2, z=128, max_batch=24)
+    oc = oracle_for(dec)
+    sig = np.full(24, codes.noise_sigma(2.0, 0.2), np.float32)
+    llr, _ = oc.gen_llr(10, 8, 0, sig, 2)
+    if qtype == "f16":
+        q = torch.from_numpy(llr.astype(np.float16))
+        wide, scale = q.float().numpy(), 1.0
+    else:
+        scale = 0.25
+        q = torch.from_numpy(np.clip(np.round(llr / scale), -128, 127).astype(np.int8))
+        wide = (q.numpy().astype(np.float32) * np.float32(scale)).astype(np.float32)
+    out = torch.empty((24, dec.packed_bytes), dtype=torch.uint8).pin_memory()
+    s = torch.cuda.Stream()
+    dec.decode_host_q(q.pin_memory(), out, 8, scale=scale, stream=s)
+    s.synchronize()
+    want, _, _ = oc.minsum_f32(wide, 8)
+    np.testing.assert_array_equal(out.numpy(), want)
