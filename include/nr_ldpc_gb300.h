@@ -212,7 +212,7 @@ int nrldpc_rm_k0(int bg, int z, int rv);
  * another runtime's memory manager -- and so cannot hold an nrldpc_handle.
  * Same results as nrldpc_decode for 5G NR (bg, z) with alpha (device
  * pointers, 16-byte aligned d_llr; packed output as nrldpc_decode).  Scratch
- * is one static 32 MiB device array in the library, held by a GPU from the
+ * is one static 96 MiB device array in the library, held by a GPU from the
  * first call on it until the process exits; a code whose per-CTA check-node
  * state does not fit returns NRLDPC_ERR_SCRATCH_TOO_SMALL.  The first call on
  * a device (the current one) sets it up: make it before any stream capture.

@@ -318,7 +318,7 @@ int nrldpc_batch_create(int device, int max_jobs, float alpha, nrldpc_batch** ou
             // default: as many codewords as 384 threads and shared memory allow
             const size_t room = b->smem_optin - kHeaderBytesBatch - kBatchTableBytes;
             int c = std::max(1, kMaxThreads / z);
-            while (c > 1 && 2ull * c * t.n_bp * 4 > room) c--;
+            while (c > 1 && group_smem_bytes(t, c) > room) c--;
             b->cpb_default[id] = b->cpb[id] = std::min(c, 48);
         }
     if (cudaMalloc(&b->d_tables, sizeof(CodeTable) * kNumCodes) != cudaSuccess ||
@@ -413,8 +413,8 @@ int nrldpc_batch_set_jobs(nrldpc_batch* batch, const nrldpc_job* jobs, int n_job
         for (int s = i; s < k; s += cpb) {
             const int cnt = std::min(cpb, k - s);
             items.push_back(WorkItem{id, s, cnt, 0});
-            slot_words = std::max(slot_words, static_cast<size_t>(cnt) * 3 * t.rows * t.z);
-            bufs = std::max(bufs, static_cast<size_t>(2) * cnt * t.n_bp * 4);
+            slot_words = std::max(slot_words, static_cast<size_t>(cnt) * 4 * t.rows * t.z);
+            bufs = std::max(bufs, group_smem_bytes(t, cnt));
         }
         i = k;
     }

@@ -74,6 +74,22 @@ bool fill_table(const int* base, int rows, int cols, int z, int kb, CodeTable* t
     }
     t->row_ptr[rows] = static_cast<uint16_t>(e);
     t->n_edges = e;
+    // Suffix columns: the longest run of trailing columns that each have one
+    // edge, in distinct rows (each is then the last edge of its row).
+    int col_deg[kMaxCols] = {0}, col_row[kMaxCols] = {0};
+    for (int r = 0; r < rows; r++)
+        for (int k = t->row_ptr[r]; k < t->row_ptr[r + 1]; k++) {
+            col_deg[t->edge_col[k]]++;
+            col_row[t->edge_col[k]] = r;
+        }
+    int n_core = cols;
+    while (n_core > 0 && col_deg[n_core - 1] == 1 && !t->row_sfx[col_row[n_core - 1]]) {
+        n_core--;
+        t->row_sfx[col_row[n_core]] = 1;
+        t->sfx_row[n_core] = static_cast<uint8_t>(col_row[n_core]);
+    }
+    t->n_core = n_core;
+    t->core_floats = (n_core * z + 3) / 4 * 4;
     // Barrier placement: greedy groups of consecutive rows that pairwise share
     // no base column; a barrier closes each group.
     int used[kMaxCols] = {0};

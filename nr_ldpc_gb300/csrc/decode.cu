@@ -1,15 +1,19 @@
 // Fused flooding normalized min-sum decoder for sm_103a.
 //
 // One CTA holds `cpb` whole codewords on chip for all iterations:
-//   * two fp32 posterior buffers per codeword in shared memory, Lold (read by
-//     the check-node pass) and Lnew (accumulates the posterior update);
-//   * the check-node state between iterations, compressed to 12 B per lifted
-//     row (min1, min2, argmin + R sign bits) as three coalesced word streams,
-//     in a per-CTA slot of global memory that stays L2-resident (each CTA
-//     reuses its slot for every codeword it takes), requested three rows
-//     ahead.
-// The LLR batch comes into shared memory with one cp.async.bulk copy per
-// codeword group (mbarrier completion, bounded wait).
+//   * two fp32 posterior buffers per codeword in shared memory over the core
+//     columns, Lold (read by the check-node pass) and Lnew (accumulates the
+//     posterior update);
+//   * the check-node state between iterations, compressed to 16 B per lifted
+//     row (min1, min2, argmin + R sign bits, and the posterior of the row's
+//     degree-1 suffix column) as one uint4 per (row, sub-row), in a per-CTA
+//     slot of global memory that stays L2-resident (each CTA reuses its slot
+//     for every codeword it takes), requested three rows ahead.  Keeping the
+//     suffix columns (5G NR: the extension parity, 42 of 68 BG1 columns) out
+//     of shared memory halves it, so two CTAs run per SM.
+// The core LLRs come into shared memory with one cp.async.bulk copy per
+// codeword (mbarrier completion, bounded wait); the suffix LLRs are read from
+// global memory by the first iteration's state fetch.
 //
 // Bit-exactness with the reference (ctarver/NR_GPU_LDPC):
 //   * check-node arithmetic of src/ldpc_kernels.cu:73-181 (first iteration)
@@ -99,28 +103,43 @@ __device__ __forceinline__ void sts(uint32_t a, float v) {
     asm volatile("st.shared.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
 }
 
+__device__ __forceinline__ void sts_u8(uint32_t a, uint32_t v) {
+    asm volatile("st.shared.u8 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
+
 // One lifted row (base row with D edges, sub-row s) of one iteration.
 // The first iteration passes a zero state (and a zero previous weight), so
 // R_old = +0 and Q = L - (+0) = L, dt = R - (+0) = R exactly, as in
 // cnp_kernel_1st_iter.  CHECK also accumulates the parity of the hard
-// decisions read from Lold (syndrome of the previous iteration).
+// decisions read (syndrome of the previous iteration).
 //   s4old: shared byte address of this slot's Lold plus 4*s;
-//   dnew:  byte distance from Lold to Lnew; z4 = 4*Z.
-//   st: this row's state from the previous iteration; st_out: where this
-//   iteration's goes (min1, then min2 and info at +rz and +2*rz words), or
-//   null in the last iteration.
+//   dnew:  byte distance from Lold to Lnew; z4 = 4*Z;
+//   sfx:   the last edge is a suffix column: its posterior is st.w (read)
+//          and goes to the stored state's w (written), not shared memory;
+//   st:    this row's state from the previous iteration; st_out: where this
+//          iteration's goes, or null;
+//   hd:    shared byte address for the suffix column's hard decisions
+//          (bit 0: posterior read, bit 1: posterior written), or 0;
+//   app_sfx: global slot for the suffix posterior read, or null.
 template <int D, bool WEIGHTED, bool CHECK>
-__device__ __forceinline__ void row_update(const CodeTable& tab, int e0, uint32_t s, uint32_t s4old,
-                                           uint32_t dnew, uint32_t z4, const float2* wpair, uint3 st,
-                                           uint32_t* st_out, uint32_t rz, float alpha, uint32_t& syn) {
+__device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sfx, uint32_t s,
+                                           uint32_t s4old, uint32_t dnew, uint32_t z4,
+                                           const float2* wpair, uint4 st, uint4* st_out, uint32_t hd,
+                                           float* app_sfx, float alpha, uint32_t& syn) {
+    constexpr int LAST = D - 1;
     uint32_t addr[D];
     float lv[D];
 #pragma unroll
     for (int i = 0; i < D; i++) {
-        uint32_t a = s4old + tab.ebase4[e0 + i];
-        if (s >= tab.ethr[e0 + i]) a -= z4;  // column (s + V) mod Z of the edge's block
-        addr[i] = a;
-        lv[i] = lds(a);
+        if (i == LAST && sfx) {
+            addr[i] = 0;
+            lv[i] = __uint_as_float(st.w);
+        } else {
+            uint32_t a = s4old + tab.ebase4[e0 + i];
+            if (s >= tab.ethr[e0 + i]) a -= z4;  // column (s + V) mod Z of the edge's block
+            addr[i] = a;
+            lv[i] = lds(a);
+        }
     }
     // old messages R_old from the previous iteration's state
     float rold[D];
@@ -160,11 +179,16 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, uint32_
         a1 = __fmul_rn(alpha, m1);
         a2 = __fmul_rn(alpha, m2);
     }
+    // Lnew read-modify-write with the loads kPipe edges ahead of the stores
+    // (fewer live registers than loading the whole row first)
+    constexpr int kPipe = 4;
     float nv[D];
 #pragma unroll
-    for (int i = 0; i < D; i++) nv[i] = lds(addr[i] + dnew);
+    for (int i = 0; i < kPipe && i < D; i++) nv[i] = (i == LAST && sfx) ? lv[i] : lds(addr[i] + dnew);
+    float sfx_new = 0.0f;
 #pragma unroll
     for (int i = 0; i < D; i++) {
+        if (i + kPipe < D) nv[i + kPipe] = (i + kPipe == LAST && sfx) ? lv[i + kPipe] : lds(addr[i + kPipe] + dnew);
         float mag;
         if (WEIGHTED)
             mag = __fmul_rn(wpair[e0 + i].y, i == idx ? m2 : m1);
@@ -172,26 +196,32 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, uint32_
             mag = i == idx ? a2 : a1;
         const float rn = __uint_as_float(__float_as_uint(mag) | ((rsign << (31 - i)) & 0x80000000u));
         const float dt = __fsub_rn(rn, rold[i]);
-        sts(addr[i] + dnew, __fadd_rn(nv[i], dt));
+        const float v = __fadd_rn(nv[i], dt);
+        if (i == LAST && sfx)
+            sfx_new = v;
+        else
+            sts(addr[i] + dnew, v);
+    }
+    if (sfx) {
+        if (hd) sts_u8(hd, (lv[LAST] > 0.0f ? 0u : 1u) | (sfx_new > 0.0f ? 0u : 2u));
+        if (app_sfx) *app_sfx = lv[LAST];
     }
     if (st_out) {
         const uint32_t info = static_cast<uint32_t>(idx) | ((rsign & ((1u << D) - 1u)) << 8);
-        __stcg(st_out, __float_as_uint(m1));
-        __stcg(st_out + rz, __float_as_uint(m2));
-        __stcg(st_out + 2 * rz, info);
+        __stcg(st_out, make_uint4(__float_as_uint(m1), __float_as_uint(m2), info, __float_as_uint(sfx_new)));
     }
 }
 
 template <bool WEIGHTED, bool CHECK>
-__device__ __forceinline__ void row_dispatch(int deg, const CodeTable& tab, int e0, uint32_t s,
+__device__ __forceinline__ void row_dispatch(int deg, const CodeTable& tab, int e0, bool sfx, uint32_t s,
                                              uint32_t s4old, uint32_t dnew, uint32_t z4,
-                                             const float2* wpair, uint3 st, uint32_t* st_out,
-                                             uint32_t rz, float alpha, uint32_t& syn) {
+                                             const float2* wpair, uint4 st, uint4* st_out, uint32_t hd,
+                                             float* app_sfx, float alpha, uint32_t& syn) {
     switch (deg) {
-#define NRLDPC_ROW_CASE(D)                                                                   \
-    case D:                                                                                  \
-        row_update<D, WEIGHTED, CHECK>(tab, e0, s, s4old, dnew, z4, wpair, st, st_out, rz, alpha, \
-                                       syn);                                                 \
+#define NRLDPC_ROW_CASE(D)                                                                         \
+    case D:                                                                                        \
+        row_update<D, WEIGHTED, CHECK>(tab, e0, sfx, s, s4old, dnew, z4, wpair, st, st_out, hd,    \
+                                       app_sfx, alpha, syn);                                       \
         break;
         NRLDPC_ROW_CASE(1) NRLDPC_ROW_CASE(2) NRLDPC_ROW_CASE(3) NRLDPC_ROW_CASE(4)
         NRLDPC_ROW_CASE(5) NRLDPC_ROW_CASE(6) NRLDPC_ROW_CASE(7) NRLDPC_ROW_CASE(8)
@@ -204,57 +234,91 @@ __device__ __forceinline__ void row_dispatch(int deg, const CodeTable& tab, int 
     }
 }
 
+// Position (c*Z + (s + V) mod Z) of sub-row s on edge e.
+__device__ __forceinline__ int edge_pos(const CodeTable& tab, int e, uint32_t s) {
+    int p = static_cast<int>(tab.edge[e] & 0xffffu) + static_cast<int>(s);
+    if (s >= tab.ethr[e]) p -= tab.z;
+    return p;
+}
+
 // Hard decisions (and optionally posterior / iteration count) of one codeword
-// slot, written by the slot's Z threads.
-__device__ __forceinline__ void write_outputs(const CodeTable& tab, const float* L, uint32_t s,
-                                              uint8_t* packed, float* app, int32_t* iters,
-                                              int it) {
-    const int n = tab.n_bp, z = tab.z;
+// slot, written by the slot's Z threads.  L: core-column posteriors in shared
+// memory; hd: the slot's suffix hard-decision bytes, bit `bit` taken; the
+// suffix posteriors come from the state slot when app_from_state (otherwise
+// the row pass already wrote them).
+__device__ __forceinline__ void write_outputs(const CodeTable& tab, const float* L, const uint8_t* hd,
+                                              int bit, const uint4* st_slot, uint32_t s, uint8_t* packed,
+                                              float* app, int32_t* iters, int it, bool app_from_state) {
+    const int n = tab.n_bp, z = tab.z, ncz = tab.n_core * z;
     for (int b = static_cast<int>(s); b < tab.packed_bytes; b += z) {
+        int pos = 8 * b;
+        int c = pos / z, p = pos - c * z;
         uint32_t v = 0;
-#pragma unroll
-        for (int i = 0; i < 8; i++) {
-            const int c = 8 * b + i;
-            if (c < n && !(L[c] > 0.0f)) v |= 1u << i;
+        for (int i = 0; i < 8 && pos < n; i++, pos++) {
+            uint32_t one;
+            if (pos < ncz) {
+                one = L[pos] > 0.0f ? 0u : 1u;
+            } else {
+                const int r = tab.sfx_row[c];
+                int sr = p - static_cast<int>(tab.edge_shift[tab.row_ptr[r + 1] - 1]);
+                if (sr < 0) sr += z;
+                one = (hd[r * z + sr] >> bit) & 1u;
+            }
+            v |= one << i;
+            if (++p == z) {
+                p = 0;
+                c++;
+            }
         }
         packed[b] = static_cast<uint8_t>(v);
     }
-    if (app)
-        for (int c = static_cast<int>(s); c < n; c += z) app[c] = L[c];
+    if (app) {
+        for (int pos = static_cast<int>(s); pos < ncz; pos += z) app[pos] = L[pos];
+        if (app_from_state)
+            for (int c = tab.n_core; c < tab.cols; c++) {
+                const int r = tab.sfx_row[c];
+                app[edge_pos(tab, tab.row_ptr[r + 1] - 1, s)] = __uint_as_float(__ldcg(&st_slot[r * z + s].w));
+            }
+    }
     if (iters && s == 0) *iters = it;
 }
 
-__device__ __forceinline__ uint3 load_state(const uint32_t* p, uint32_t rz) {
-    return make_uint3(__ldcg(p), __ldcg(p + rz), __ldcg(p + 2 * rz));
-}
-
 // All base rows of one iteration, ascending; returns the OR of the row
-// parities of the hard decisions read (CHECK only).  The check-node state of
-// row r+3 is requested while row r runs (L2 latency spans several rows).
-// State layout per CTA slot: min1[rows*Z], min2[rows*Z], info[rows*Z].
+// parities of the hard decisions read (CHECK only).  The state of row r+3 is
+// requested while row r runs (L2 latency spans several rows); in the first
+// iteration the state is zero and only the suffix posterior is fetched, from
+// the codeword's LLRs in global memory.
+//   store: write this iteration's state; write_hd: write the suffix hard
+//   decisions; app_cw: the codeword's posterior output when the suffix
+//   posteriors read are to be written there.
 template <bool WEIGHTED, bool CHECK>
 __device__ __forceinline__ uint32_t iterate_rows(const CodeTable& tab, uint32_t s, uint32_t s4old,
-                                                 uint32_t dnew, const float2* wpair, uint32_t* st_base,
-                                                 bool act, bool first, bool last, float alpha) {
+                                                 uint32_t dnew, const float2* wpair, uint4* st_base,
+                                                 const float* gllr, uint32_t hd_base, float* app_cw,
+                                                 bool act, bool first, bool store, bool write_hd,
+                                                 float alpha) {
     const int z = tab.z, rows = tab.rows;
-    const uint32_t z4 = 4u * static_cast<uint32_t>(z), rz = static_cast<uint32_t>(rows * z);
+    const uint32_t z4 = 4u * static_cast<uint32_t>(z);
     uint32_t fail = 0;
-    const uint3 zero = make_uint3(0u, 0u, 0u);
-    const bool pf = !first && act;
-    uint3 s0 = zero, s1 = zero, s2 = zero;
-    if (pf) {
-        s0 = load_state(st_base + s, rz);
-        s1 = load_state(st_base + min(1, rows - 1) * z + s, rz);
-        s2 = load_state(st_base + min(2, rows - 1) * z + s, rz);
-    }
+    auto fetch = [&](int r) -> uint4 {
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (!act || r >= rows) return v;
+        if (!first) return __ldcg(st_base + r * z + s);
+        if (tab.row_sfx[r]) v.w = __float_as_uint(__ldcs(gllr + edge_pos(tab, tab.row_ptr[r + 1] - 1, s)));
+        return v;
+    };
+    uint4 s0 = fetch(0), s1 = fetch(1), s2 = fetch(2);
     for (int r = 0; r < rows; r++) {
-        uint3 s3 = zero;
-        if (pf) s3 = load_state(st_base + min(r + 3, rows - 1) * z + s, rz);
+        const uint4 s3 = fetch(r + 3);
         if (act) {
+            const bool sfx = tab.row_sfx[r] != 0;
+            const int e0 = tab.row_ptr[r];
+            float* app_sfx = (app_cw && sfx) ? app_cw + edge_pos(tab, tab.row_ptr[r + 1] - 1, s) : nullptr;
             uint32_t syn = 0;
-            row_dispatch<WEIGHTED, CHECK>(tab.row_deg[r], tab, tab.row_ptr[r], s, s4old, dnew, z4,
-                                          wpair, s0, last ? nullptr : st_base + r * z + s, rz,
-                                          alpha, syn);
+            row_dispatch<WEIGHTED, CHECK>(tab.row_deg[r], tab, e0, sfx, s, s4old, dnew, z4, wpair, s0,
+                                          store ? st_base + r * z + s : nullptr,
+                                          (write_hd && sfx) ? hd_base + static_cast<uint32_t>(r * z) : 0u,
+                                          app_sfx, alpha, syn);
             fail |= syn;
         }
         s0 = s1;
@@ -272,20 +336,24 @@ struct SlotOut {
     int32_t* iters;
 };
 
-// All iterations of one codeword group already loaded into buf0 (Lold):
-// cpb slots, this thread = sub-row s of slot `slot`.  Ends with a barrier.
+// All iterations of one codeword group whose core LLRs are already in buf0
+// (Lold): cpb slots, this thread = sub-row s of slot `slot`; gllr = the
+// slot's codeword in global memory (suffix LLRs).  Ends with a barrier.
 template <bool WEIGHTED>
 __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slot, uint32_t s,
-                                          bool slot_done, float* buf0, float2* wpair, int* s_fail,
-                                          uint32_t* st_base, SlotOut out, int n_iter, int early_stop,
-                                          float alpha, const float* weights, int n_w_iters) {
-    const int z = tab.z, n = tab.n_bp, tid = threadIdx.x;
-    float* lold = buf0 + static_cast<size_t>(slot) * n;  // read by the check-node pass
-    float* lnew = lold + static_cast<size_t>(cpb) * n;   // accumulates the new posterior
+                                          bool slot_done, float* buf0, uint8_t* hd0, float2* wpair,
+                                          int* s_fail, uint4* st_base, const float* gllr, SlotOut out,
+                                          int n_iter, int early_stop, float alpha, const float* weights,
+                                          int n_w_iters) {
+    const int z = tab.z, cf = tab.core_floats, tid = threadIdx.x;
+    float* lold = buf0 + static_cast<size_t>(slot) * cf;  // read by the check-node pass
+    float* lnew = lold + static_cast<size_t>(cpb) * cf;   // accumulates the new posterior
+    const uint8_t* hd = hd0 + static_cast<size_t>(slot) * tab.rows * z;
     const uint32_t s4old = smem_addr(lold) + 4u * s;
-    const uint32_t dnew = static_cast<uint32_t>(cpb) * static_cast<uint32_t>(n) * 4u;
+    const uint32_t dnew = static_cast<uint32_t>(cpb) * static_cast<uint32_t>(cf) * 4u;
+    const uint32_t hd_base = smem_addr(hd) + s;
     if (!slot_done)
-        for (int k = static_cast<int>(s); k < n / 4; k += z)
+        for (int k = static_cast<int>(s); k < cf / 4; k += z)
             reinterpret_cast<float4*>(lnew)[k] = reinterpret_cast<const float4*>(lold)[k];
     for (int t = 0; t < n_iter; t++) {
         const bool first = t == 0, last = t == n_iter - 1;
@@ -299,26 +367,29 @@ __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slo
         __syncthreads();
         const bool act = !slot_done;
         const bool check = early_stop && t > 0;
+        const bool store = !last || out.app != nullptr;
+        const bool write_hd = check || last;
+        float* app_cw = (check && out.app) ? out.app : nullptr;
         const uint32_t fail =
-            check ? iterate_rows<WEIGHTED, true>(tab, s, s4old, dnew, wpair, st_base, act, first, last,
-                                                alpha)
-                  : iterate_rows<WEIGHTED, false>(tab, s, s4old, dnew, wpair, st_base, act, first, last,
-                                                 alpha);
+            check ? iterate_rows<WEIGHTED, true>(tab, s, s4old, dnew, wpair, st_base, gllr, hd_base, app_cw,
+                                                act, first, store, write_hd, alpha)
+                  : iterate_rows<WEIGHTED, false>(tab, s, s4old, dnew, wpair, st_base, gllr, hd_base, app_cw,
+                                                 act, first, store, write_hd, alpha);
         if (check) {
             if (act && fail) atomicOr(&s_fail[slot], 1);
             __syncthreads();
             const bool conv = act && s_fail[slot] == 0;
             if (conv)  // HD of the previous iteration is a codeword
-                write_outputs(tab, lold, s, out.packed, out.app, out.iters, t);
+                write_outputs(tab, lold, hd, 0, st_base, s, out.packed, out.app, out.iters, t, false);
             slot_done = slot_done || conv;
             if (__syncthreads_and(slot_done)) break;
         }
         if (last) {
-            if (!slot_done) write_outputs(tab, lnew, s, out.packed, out.app, out.iters, n_iter);
+            if (!slot_done) write_outputs(tab, lnew, hd, 1, st_base, s, out.packed, out.app, out.iters, n_iter, true);
             break;
         }
         if (!slot_done)  // the posterior just accumulated is the next iteration's input
-            for (int k = static_cast<int>(s); k < n / 4; k += z)
+            for (int k = static_cast<int>(s); k < cf / 4; k += z)
                 reinterpret_cast<float4*>(lold)[k] = reinterpret_cast<const float4*>(lnew)[k];
     }
     __syncthreads();  // buffers are rewritten by the next group's copy
@@ -334,16 +405,16 @@ __global__ void __launch_bounds__(kMaxThreads, MINB)
     int* s_group = reinterpret_cast<int*>(smem + 8);
     int* s_fail = reinterpret_cast<int*>(smem + 16);
     float2* wpair = reinterpret_cast<float2*>(smem + kHeaderBytes);
-    const int wbytes = WEIGHTED ? kMaxEdges * 8 : 0;
-    float* buf0 = reinterpret_cast<float*>(smem + kHeaderBytes + wbytes);
+    float* buf0 = reinterpret_cast<float*>(smem + kHeaderBytes + kMaxEdges * 8);
 
-    const int z = tab.z, n = tab.n_bp, cpb = a.cpb, rows = tab.rows;
+    const int z = tab.z, n = tab.n_bp, cpb = a.cpb, rows = tab.rows, cf = tab.core_floats;
+    uint8_t* hd0 = reinterpret_cast<uint8_t*>(buf0 + 2 * static_cast<size_t>(cpb) * cf);
     const int tid = threadIdx.x;
     const int slot = tid / z;
     const uint32_t s = static_cast<uint32_t>(tid - slot * z);
     const bool valid_thread = slot < cpb;
-    uint32_t* st_base =
-        a.state + (static_cast<size_t>(blockIdx.x) * cpb + (valid_thread ? slot : 0)) * 3 * rows * z;
+    uint4* st_base = reinterpret_cast<uint4*>(a.state) +
+                     (static_cast<size_t>(blockIdx.x) * cpb + (valid_thread ? slot : 0)) * rows * z;
 
     if (tid == 0) {
         mbar_init(bar, 1);
@@ -359,11 +430,12 @@ __global__ void __launch_bounds__(kMaxThreads, MINB)
         if (g >= a.n_groups) break;
         const int cw0 = g * cpb;
         const int n_valid = min(cpb, a.n_cw - cw0);
-        if (tid == 0) {
+        if (tid == 0) {  // core-column LLRs of each codeword into its Lold
             fence_proxy_async();
-            const uint32_t bytes = static_cast<uint32_t>(n_valid) * n * 4u;
-            mbar_arrive_expect_tx(bar, bytes);
-            bulk_g2s(smem_addr(buf0), a.llr + static_cast<size_t>(cw0) * n, bytes, bar);
+            mbar_arrive_expect_tx(bar, static_cast<uint32_t>(n_valid) * cf * 4u);
+            for (int k = 0; k < n_valid; k++)
+                bulk_g2s(smem_addr(buf0 + static_cast<size_t>(k) * cf), a.llr + static_cast<size_t>(cw0 + k) * n,
+                         cf * 4u, bar);
         }
         bool ok = mbar_wait_bounded(bar, phase);
         if (!__syncthreads_and(ok)) {
@@ -376,8 +448,8 @@ __global__ void __launch_bounds__(kMaxThreads, MINB)
         const size_t cw = static_cast<size_t>(cw0 + (slot_done ? 0 : slot));
         SlotOut out{a.packed + cw * tab.packed_bytes, a.app ? a.app + cw * n : nullptr,
                     a.iters ? a.iters + cw : nullptr};
-        run_group<WEIGHTED>(tab, cpb, slot, s, slot_done, buf0, wpair, s_fail, st_base, out, a.n_iter,
-                            a.early_stop, a.alpha, a.weights, a.n_w_iters);
+        run_group<WEIGHTED>(tab, cpb, slot, s, slot_done, buf0, hd0, wpair, s_fail, st_base, a.llr + cw * n, out,
+                            a.n_iter, a.early_stop, a.alpha, a.weights, a.n_w_iters);
     }
 }
 
@@ -385,7 +457,7 @@ __global__ void __launch_bounds__(kMaxThreads, MINB)
 // codes.  Each item = up to cpb codewords of one code; the item's code table
 // is copied into shared memory and every codeword is fetched from its own
 // offset with its own bulk copy.
-__global__ void __launch_bounds__(kMaxThreads, 1)
+__global__ void __launch_bounds__(kMaxThreads, 2)
     batch_decode_kernel(const __grid_constant__ BatchDecodeArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     const uint32_t bar = smem_addr(smem);
@@ -413,16 +485,17 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
         }
         __syncthreads();
         const CodeTable& tab = *stab;
-        const int z = tab.z, n = tab.n_bp, cpb = item.count;
+        const int z = tab.z, cf = tab.core_floats, cpb = item.count;
+        uint8_t* hd0 = reinterpret_cast<uint8_t*>(buf0 + 2 * static_cast<size_t>(cpb) * cf);
         const int slot = tid / z;
         const uint32_t s = static_cast<uint32_t>(tid - slot * z);
         const bool valid_thread = slot < cpb;
         if (tid == 0) {
             fence_proxy_async();
-            mbar_arrive_expect_tx(bar, static_cast<uint32_t>(cpb) * n * 4u);
+            mbar_arrive_expect_tx(bar, static_cast<uint32_t>(cpb) * cf * 4u);
             for (int k = 0; k < cpb; k++) {
                 const nrldpc_job& j = a.jobs[a.order[item.start + k]];
-                bulk_g2s(smem_addr(buf0 + static_cast<size_t>(k) * n), a.llr + j.llr_offset, n * 4u, bar);
+                bulk_g2s(smem_addr(buf0 + static_cast<size_t>(k) * cf), a.llr + j.llr_offset, cf * 4u, bar);
             }
         }
         bool ok = mbar_wait_bounded(bar, phase);
@@ -435,18 +508,17 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
         const int jidx = valid_thread ? a.order[item.start + slot] : 0;
         const nrldpc_job& job = a.jobs[jidx];
         SlotOut out{a.packed + job.out_offset, nullptr, a.iters ? a.iters + jidx : nullptr};
-        uint32_t* st_base = a.state + static_cast<size_t>(blockIdx.x) * a.slot_words +
-                            static_cast<size_t>(valid_thread ? slot : 0) * 3 * tab.rows * z;
-        run_group<false>(tab, cpb, slot, s, !valid_thread, buf0, nullptr, s_fail, st_base, out, a.n_iter,
-                         a.early_stop, a.alpha, nullptr, 1);
+        uint4* st_base = reinterpret_cast<uint4*>(a.state + static_cast<size_t>(blockIdx.x) * a.slot_words) +
+                         static_cast<size_t>(valid_thread ? slot : 0) * tab.rows * z;
+        run_group<false>(tab, cpb, slot, s, !valid_thread, buf0, hd0, nullptr, s_fail, st_base,
+                         a.llr + job.llr_offset, out, a.n_iter, a.early_stop, a.alpha, nullptr, 1);
     }
 }
 
 }  // namespace
 
 size_t decode_smem_bytes(const CodeTable& tab, int cpb) {
-    return kHeaderBytes + static_cast<size_t>(kMaxEdges) * 8 +
-           2 * static_cast<size_t>(cpb) * tab.n_bp * sizeof(float);
+    return kHeaderBytes + static_cast<size_t>(kMaxEdges) * 8 + group_smem_bytes(tab, cpb);
 }
 
 template <bool W, int MINB>

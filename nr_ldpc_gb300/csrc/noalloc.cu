@@ -10,9 +10,9 @@
 // passes only its input and output buffers, and the decoder's scratch lives in
 // a fixed static device array of this file.
 //
-// Scratch: kNoAllocScratchBytes (32 MiB) for the check-node state of the
-// persistent decode CTAs, enough for one CTA per SM of a 152-SM GB300 at the
-// largest code (BG1, Z = 384: 211,968 bytes per CTA), plus 256 bytes of
+// Scratch: kNoAllocScratchBytes (96 MiB) for the check-node state of the
+// persistent decode CTAs, enough for two CTAs per SM of a 152-SM GB300 at the
+// largest code (BG1, Z = 384: 282,624 bytes per CTA), plus 256 bytes of
 // counters.  A GPU holds this memory from the first call of this entry point
 // on it (module load) until the process exits.
 //
@@ -35,7 +35,7 @@
 namespace nrldpc {
 namespace {
 
-constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;
+constexpr size_t kNoAllocScratchBytes = size_t(96) << 20;
 constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_state[kNoAllocScratchBytes];

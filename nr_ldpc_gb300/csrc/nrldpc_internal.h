@@ -20,10 +20,19 @@ constexpr int kMaxThreads = 384;  // decode CTA size bound (cw_per_cta * Z)
 struct alignas(16) CodeTable {
     int rows, cols, z, n_edges, n_bp, packed_bytes;
     int kb;                        // systematic base columns (encoder)
+    // Base columns [n_core, cols) are suffix columns: each has degree 1 and is
+    // the last edge of its row, and no row has two.  (5G NR: the extension
+    // parity columns, 42 of 68 in BG1, 38 of 52 in BG2.)  The decoder keeps
+    // their posteriors in the owning row's check-node state instead of in
+    // shared memory.
+    int n_core;
+    int core_floats;               // n_core * Z rounded up to a multiple of 4
     uint16_t row_ptr[kMaxRows + 1];
     uint8_t row_deg[kMaxRows];
     uint8_t sync_after[kMaxRows];  // 1: CTA barrier after this row (row groups
                                    // between barriers share no base column)
+    uint8_t row_sfx[kMaxRows];     // 1: the row's last edge is a suffix column
+    uint8_t sfx_row[kMaxCols];     // suffix column -> its row
     // per edge, row-major ascending (row, then column) = the reference's
     // h_compact1 order: low 16 bits blk_col*Z + V, high 16 bits Z - V
     uint32_t edge[kMaxEdges];
@@ -36,16 +45,17 @@ struct alignas(16) CodeTable {
     uint16_t edge_shift[kMaxEdges];  // V mod Z
 };
 
-// Check-node state of one lifted row, kept between iterations (12 B): min1
-// (raw |Q|), min2, info = idx (bits 0..4) | R sign of edge i at bit 8+i,
-// stored as three arrays per CTA slot: [slot][3][rows * Z] words.
-constexpr size_t kStateBytesPerRow = 12;
+// Check-node state of one lifted row, kept between iterations (16 B, one
+// uint4 per (row, sub-row), [slot][rows][Z]): min1 (raw |Q|), min2,
+// info = idx (bits 0..4) | R sign of edge i at bit 8+i, and the posterior of
+// the row's suffix column at this sub-row (unused in rows without one).
+constexpr size_t kStateBytesPerRow = 16;
 struct DecodeArgs {
     const float* llr;
     uint8_t* packed;
     float* app;
     int32_t* iters;
-    uint32_t* state;        // [grid * cpb][3][rows * Z]
+    uint32_t* state;        // [grid * cpb][rows * Z][4]
     int* work_counter;      // dynamic codeword-group scheduler, zeroed per launch
     int* error_flag;        // bounded-wait failures
     const float* weights;   // [n_w_iters][n_edges] or null
@@ -76,10 +86,17 @@ struct BatchDecodeArgs {
     uint32_t* state;            // [grid][slot_words]
     int* work_counter;
     int* error_flag;
-    size_t slot_words;          // state words per CTA (largest cpb * 3 * rows * Z)
+    size_t slot_words;          // state words per CTA (largest cpb * 4 * rows * Z)
     int n_items, n_iter, early_stop;
     float alpha;
 };
+// Shared memory of one decode group of cpb codewords: Lold and Lnew over the
+// core columns, plus one hard-decision byte per lifted row for the suffix
+// columns.
+inline size_t group_smem_bytes(const CodeTable& t, int cpb) {
+    const size_t hd = (static_cast<size_t>(cpb) * t.rows * t.z + 15) / 16 * 16;
+    return 2 * static_cast<size_t>(cpb) * t.core_floats * sizeof(float) + hd;
+}
 cudaError_t launch_batch_decode(const BatchDecodeArgs& args, int grid, size_t smem, cudaStream_t stream);
 const void* batch_decode_kernel_ptr();
 
