@@ -127,6 +127,18 @@ int nrldpc_decode_weighted(nrldpc_handle* h, const float* d_llr, uint8_t* d_pack
                            int n_iter, int early_stop, float* d_app, int32_t* d_iters,
                            nrldpc_stream_t stream);
 
+/* Message-passing schedule of a handle's decodes (nrldpc_decode,
+ * nrldpc_decode_weighted, the host-buffer calls).  FLOODING (default) is the
+ * reference's: every check row reads the previous iteration's posterior
+ * (src/gpu_decoder_top.cu:25-49).  LAYERED has no reference counterpart:
+ * base rows run in ascending order and each updates the posterior in place
+ * (Q = A - R_old, A = Q + R_new), so later rows of an iteration see earlier
+ * rows' messages; it converges in about 0.6x the iterations.  With early stop
+ * a layered decode checks the syndrome after each iteration and reports
+ * d_iters = iterations run. */
+enum { NRLDPC_SCHEDULE_FLOODING = 0, NRLDPC_SCHEDULE_LAYERED = 1 };
+int nrldpc_set_schedule(nrldpc_handle* h, int schedule);
+
 /* ---- learned weighted min-sum training (no reference counterpart) ----------
  * Model: R^t_e = w[t][e] * sign * min (weights per iteration t < n_iter and
  * base edge e, shared by all lifted copies); posterior as the decoder;

@@ -37,6 +37,7 @@ struct Handle {
     float* weights = nullptr;
     int n_w_iters = 0;
     bool wms_ready = false;
+    int schedule = NRLDPC_SCHEDULE_FLOODING;
 };
 
 int map_cuda(cudaError_t e) { return e == cudaSuccess ? NRLDPC_OK : NRLDPC_ERR_CUDA; }
@@ -228,7 +229,8 @@ int decode_impl(Handle* h, const float* llr, uint8_t* packed, int n_cw, int n_it
     const int grid = std::min(a.n_groups, h->max_grid);
     cudaError_t e = cudaMemsetAsync(h->scratch, 0, sizeof(int), stream);
     if (e != cudaSuccess) return NRLDPC_ERR_CUDA;
-    return map_cuda(launch_decode(h->tab, a, grid, h->threads, h->smem, weighted, h->minb, stream));
+    return map_cuda(launch_decode(h->tab, a, grid, h->threads, h->smem, weighted,
+                                  h->schedule == NRLDPC_SCHEDULE_LAYERED, h->minb, stream));
 }
 
 }  // namespace
@@ -425,6 +427,14 @@ int nrldpc_decode_host_async_q(nrldpc_handle* handle, const void* h_llr_q, int q
                                     cudaMemcpyDeviceToHost, s));
 }
 
+int nrldpc_set_schedule(nrldpc_handle* handle, int schedule) {
+    Handle* h = reinterpret_cast<Handle*>(handle);
+    if (!h || (schedule != NRLDPC_SCHEDULE_FLOODING && schedule != NRLDPC_SCHEDULE_LAYERED))
+        return NRLDPC_ERR_INVALID_ARG;
+    h->schedule = schedule;
+    return NRLDPC_OK;
+}
+
 int nrldpc_set_weights(nrldpc_handle* handle, const float* w, int n_w_iters) {
     Handle* h = reinterpret_cast<Handle*>(handle);
     if (!h || n_w_iters < 0 || (n_w_iters > 0 && !w)) return NRLDPC_ERR_INVALID_ARG;
@@ -442,16 +452,22 @@ int nrldpc_set_weights(nrldpc_handle* handle, const float* w, int n_w_iters) {
 // ---- learned weighted min-sum training --------------------------------------------------
 namespace {
 struct WmsLayout {
-    size_t states, gseed, gq, total;
+    size_t states, gseed, gq, gh, total;
 };
+// Workspace: per-iteration states and loss seeds, the flooding adjoint's
+// per-row dloss/dQ, and (layered schedule) the per-edge dloss/dR.
 WmsLayout wms_layout(const Handle* h, int n_cw, int n_iter) {
     auto up = [](size_t x) { return (x + 255) / 256 * 256; };
     WmsLayout l;
     const size_t rz = static_cast<size_t>(h->tab.rows) * h->tab.z;
+    const size_t slots = static_cast<size_t>(h->sm_count) * h->cpb;
     l.states = up(static_cast<size_t>(n_iter) * n_cw * rz * sizeof(uint4));
     l.gseed = up(static_cast<size_t>(n_iter) * n_cw * h->tab.n_bp * sizeof(float));
-    l.gq = up(static_cast<size_t>(h->sm_count) * h->cpb * rz * sizeof(uint4));
-    l.total = l.states + l.gseed + l.gq;
+    l.gq = up(slots * rz * sizeof(uint4));
+    l.gh = h->schedule == NRLDPC_SCHEDULE_LAYERED
+               ? up(slots * static_cast<size_t>(h->tab.n_edges) * h->tab.z * sizeof(float))
+               : 0;
+    l.total = l.states + l.gseed + l.gq + l.gh;
     return l;
 }
 int wms_check(Handle* h, int n_cw, int n_iter) {
@@ -484,9 +500,12 @@ int nrldpc_wms_forward(nrldpc_handle* handle, const float* d_llr, const uint8_t*
     char* ws = static_cast<char*>(d_workspace);
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     if (cudaMemsetAsync(h->scratch, 0, sizeof(int), st) != cudaSuccess) return NRLDPC_ERR_CUDA;
-    return map_cuda(launch_wms(false, h->tab, d_llr, d_cw_packed, d_weights,
+    const bool lay = h->schedule == NRLDPC_SCHEDULE_LAYERED;
+    return map_cuda(launch_wms(false, lay, h->tab, d_llr, d_cw_packed, d_weights,
                                reinterpret_cast<uint4*>(ws), reinterpret_cast<float*>(ws + l.states),
-                               reinterpret_cast<uint4*>(ws + l.states + l.gseed), d_loss, nullptr,
+                               reinterpret_cast<uint4*>(ws + l.states + l.gseed),
+                               lay ? reinterpret_cast<float*>(ws + l.states + l.gseed + l.gq) : nullptr,
+                               d_loss, nullptr,
                                d_app, h->scratch, n_cw, n_iter, h->cpb, h->sm_count, h->threads,
                                wms_smem_bytes(h->tab, h->cpb), loss_scale, st));
 }
@@ -501,9 +520,12 @@ int nrldpc_wms_backward(nrldpc_handle* handle, int n_cw, int n_iter, const float
     char* ws = static_cast<char*>(d_workspace);
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     if (cudaMemsetAsync(h->scratch, 0, sizeof(int), st) != cudaSuccess) return NRLDPC_ERR_CUDA;
-    return map_cuda(launch_wms(true, h->tab, nullptr, nullptr, d_weights, reinterpret_cast<uint4*>(ws),
+    const bool lay = h->schedule == NRLDPC_SCHEDULE_LAYERED;
+    return map_cuda(launch_wms(true, lay, h->tab, nullptr, nullptr, d_weights, reinterpret_cast<uint4*>(ws),
                                reinterpret_cast<float*>(ws + l.states),
-                               reinterpret_cast<uint4*>(ws + l.states + l.gseed), nullptr, d_grad,
+                               reinterpret_cast<uint4*>(ws + l.states + l.gseed),
+                               lay ? reinterpret_cast<float*>(ws + l.states + l.gseed + l.gq) : nullptr,
+                               nullptr, d_grad,
                                nullptr, h->scratch, n_cw, n_iter, h->cpb, h->sm_count, h->threads,
                                wms_smem_bytes(h->tab, h->cpb), 0.0f, st));
 }

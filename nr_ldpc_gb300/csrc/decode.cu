@@ -106,6 +106,11 @@ __device__ __forceinline__ void sts(uint32_t a, float v) {
 __device__ __forceinline__ void sts_u8(uint32_t a, uint32_t v) {
     asm volatile("st.shared.u8 [%0], %1;" ::"r"(a), "r"(v) : "memory");
 }
+__device__ __forceinline__ uint32_t lds_u8(uint32_t a) {
+    uint32_t v;
+    asm volatile("ld.shared.u8 %0, [%1];" : "=r"(v) : "r"(a));
+    return v;
+}
 
 // One lifted row (base row with D edges, sub-row s) of one iteration.
 // The first iteration passes a zero state (and a zero previous weight), so
@@ -121,7 +126,9 @@ __device__ __forceinline__ void sts_u8(uint32_t a, uint32_t v) {
 //   hd:    shared byte address for the suffix column's hard decisions
 //          (bit 0: posterior read, bit 1: posterior written), or 0;
 //   app_sfx: global slot for the suffix posterior read, or null.
-template <int D, bool WEIGHTED, bool CHECK>
+// LAYERED (no reference counterpart): one posterior buffer updated in place,
+// A = Q + R_new (dnew = 0), instead of Lnew += R_new - R_old.
+template <int D, bool WEIGHTED, bool CHECK, bool LAYERED>
 __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sfx, uint32_t s,
                                            uint32_t s4old, uint32_t dnew, uint32_t z4,
                                            const float2* wpair, uint4 st, uint4* st_out, uint32_t hd,
@@ -141,8 +148,9 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
             lv[i] = lds(a);
         }
     }
-    // old messages R_old from the previous iteration's state
-    float rold[D];
+    // old messages R_old from the previous iteration's state; kept per edge:
+    // R_old (flooding, for dt) or Q (layered, for A = Q + R_new)
+    float keep[D];
     const float om1 = __uint_as_float(st.x), om2 = __uint_as_float(st.y);
     const uint32_t oinfo = st.z;
     const int oidx = static_cast<int>(oinfo & 31u);
@@ -162,8 +170,8 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
         else
             mag = i == oidx ? oa2 : oa1;
         const float ro = __uint_as_float(__float_as_uint(mag) | ((oinfo << (23 - i)) & 0x80000000u));
-        rold[i] = ro;
         const float q = __fsub_rn(lv[i], ro);
+        keep[i] = LAYERED ? q : ro;
         if (CHECK) syn ^= (lv[i] > 0.0f) ? 0u : 1u;  // hard decision of the posterior read
         const float qa = fabsf(q);
         if (q < 0.0f) qmask |= 1u << i;
@@ -179,28 +187,45 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
         a1 = __fmul_rn(alpha, m1);
         a2 = __fmul_rn(alpha, m2);
     }
-    // Lnew read-modify-write with the loads kPipe edges ahead of the stores
-    // (fewer live registers than loading the whole row first)
-    constexpr int kPipe = 4;
-    float nv[D];
-#pragma unroll
-    for (int i = 0; i < kPipe && i < D; i++) nv[i] = (i == LAST && sfx) ? lv[i] : lds(addr[i] + dnew);
     float sfx_new = 0.0f;
+    if (LAYERED) {
 #pragma unroll
-    for (int i = 0; i < D; i++) {
-        if (i + kPipe < D) nv[i + kPipe] = (i + kPipe == LAST && sfx) ? lv[i + kPipe] : lds(addr[i + kPipe] + dnew);
-        float mag;
-        if (WEIGHTED)
-            mag = __fmul_rn(wpair[e0 + i].y, i == idx ? m2 : m1);
-        else
-            mag = i == idx ? a2 : a1;
-        const float rn = __uint_as_float(__float_as_uint(mag) | ((rsign << (31 - i)) & 0x80000000u));
-        const float dt = __fsub_rn(rn, rold[i]);
-        const float v = __fadd_rn(nv[i], dt);
-        if (i == LAST && sfx)
-            sfx_new = v;
-        else
-            sts(addr[i] + dnew, v);
+        for (int i = 0; i < D; i++) {
+            float mag;
+            if (WEIGHTED)
+                mag = __fmul_rn(wpair[e0 + i].y, i == idx ? m2 : m1);
+            else
+                mag = i == idx ? a2 : a1;
+            const float rn = __uint_as_float(__float_as_uint(mag) | ((rsign << (31 - i)) & 0x80000000u));
+            const float v = __fadd_rn(keep[i], rn);
+            if (i == LAST && sfx)
+                sfx_new = v;
+            else
+                sts(addr[i], v);
+        }
+    } else {
+        // Lnew read-modify-write with the loads kPipe edges ahead of the stores
+        // (fewer live registers than loading the whole row first)
+        constexpr int kPipe = 4;
+        float nv[D];
+#pragma unroll
+        for (int i = 0; i < kPipe && i < D; i++) nv[i] = (i == LAST && sfx) ? lv[i] : lds(addr[i] + dnew);
+#pragma unroll
+        for (int i = 0; i < D; i++) {
+            if (i + kPipe < D) nv[i + kPipe] = (i + kPipe == LAST && sfx) ? lv[i + kPipe] : lds(addr[i + kPipe] + dnew);
+            float mag;
+            if (WEIGHTED)
+                mag = __fmul_rn(wpair[e0 + i].y, i == idx ? m2 : m1);
+            else
+                mag = i == idx ? a2 : a1;
+            const float rn = __uint_as_float(__float_as_uint(mag) | ((rsign << (31 - i)) & 0x80000000u));
+            const float dt = __fsub_rn(rn, keep[i]);
+            const float v = __fadd_rn(nv[i], dt);
+            if (i == LAST && sfx)
+                sfx_new = v;
+            else
+                sts(addr[i] + dnew, v);
+        }
     }
     if (sfx) {
         if (hd) sts_u8(hd, (lv[LAST] > 0.0f ? 0u : 1u) | (sfx_new > 0.0f ? 0u : 2u));
@@ -212,7 +237,7 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
     }
 }
 
-template <bool WEIGHTED, bool CHECK>
+template <bool WEIGHTED, bool CHECK, bool LAYERED>
 __device__ __forceinline__ void row_dispatch(int deg, const CodeTable& tab, int e0, bool sfx, uint32_t s,
                                              uint32_t s4old, uint32_t dnew, uint32_t z4,
                                              const float2* wpair, uint4 st, uint4* st_out, uint32_t hd,
@@ -220,8 +245,8 @@ __device__ __forceinline__ void row_dispatch(int deg, const CodeTable& tab, int 
     switch (deg) {
 #define NRLDPC_ROW_CASE(D)                                                                         \
     case D:                                                                                        \
-        row_update<D, WEIGHTED, CHECK>(tab, e0, sfx, s, s4old, dnew, z4, wpair, st, st_out, hd,    \
-                                       app_sfx, alpha, syn);                                       \
+        row_update<D, WEIGHTED, CHECK, LAYERED>(tab, e0, sfx, s, s4old, dnew, z4, wpair, st, st_out, \
+                                                hd, app_sfx, alpha, syn);                          \
         break;
         NRLDPC_ROW_CASE(1) NRLDPC_ROW_CASE(2) NRLDPC_ROW_CASE(3) NRLDPC_ROW_CASE(4)
         NRLDPC_ROW_CASE(5) NRLDPC_ROW_CASE(6) NRLDPC_ROW_CASE(7) NRLDPC_ROW_CASE(8)
@@ -291,7 +316,7 @@ __device__ __forceinline__ void write_outputs(const CodeTable& tab, const float*
 //   store: write this iteration's state; write_hd: write the suffix hard
 //   decisions; app_cw: the codeword's posterior output when the suffix
 //   posteriors read are to be written there.
-template <bool WEIGHTED, bool CHECK>
+template <bool WEIGHTED, bool CHECK, bool LAYERED>
 __device__ __forceinline__ uint32_t iterate_rows(const CodeTable& tab, uint32_t s, uint32_t s4old,
                                                  uint32_t dnew, const float2* wpair, uint4* st_base,
                                                  const float* gllr, uint32_t hd_base, float* app_cw,
@@ -315,7 +340,7 @@ __device__ __forceinline__ uint32_t iterate_rows(const CodeTable& tab, uint32_t 
             const int e0 = tab.row_ptr[r];
             float* app_sfx = (app_cw && sfx) ? app_cw + edge_pos(tab, tab.row_ptr[r + 1] - 1, s) : nullptr;
             uint32_t syn = 0;
-            row_dispatch<WEIGHTED, CHECK>(tab.row_deg[r], tab, e0, sfx, s, s4old, dnew, z4, wpair, s0,
+            row_dispatch<WEIGHTED, CHECK, LAYERED>(tab.row_deg[r], tab, e0, sfx, s, s4old, dnew, z4, wpair, s0,
                                           store ? st_base + r * z + s : nullptr,
                                           (write_hd && sfx) ? hd_base + static_cast<uint32_t>(r * z) : 0u,
                                           app_sfx, alpha, syn);
@@ -329,6 +354,30 @@ __device__ __forceinline__ uint32_t iterate_rows(const CodeTable& tab, uint32_t 
     return fail;
 }
 
+// Syndrome of the slot's hard decisions after a layered iteration: sets
+// *fail when a lifted check is unsatisfied.  Core columns are read from the
+// posterior buffer, suffix columns from bit 1 of their hard-decision bytes.
+// Threads stop at the first failure seen by any thread of the slot.
+__device__ __forceinline__ void check_rows(const CodeTable& tab, uint32_t s, uint32_t s4a, uint32_t hd_base,
+                                           volatile int* fail) {
+    const int z = tab.z;
+    const uint32_t z4 = 4u * static_cast<uint32_t>(z);
+    for (int r = 0; r < tab.rows; r++) {
+        if (*fail) return;
+        const int e0 = tab.row_ptr[r], e1 = tab.row_ptr[r + 1] - (tab.row_sfx[r] ? 1 : 0);
+        uint32_t par = tab.row_sfx[r] ? (lds_u8(hd_base + static_cast<uint32_t>(r * z)) >> 1) & 1u : 0u;
+        for (int e = e0; e < e1; e++) {
+            uint32_t a = s4a + tab.ebase4[e];
+            if (s >= tab.ethr[e]) a -= z4;
+            par ^= lds(a) > 0.0f ? 0u : 1u;
+        }
+        if (par) {
+            *fail = 1;
+            return;
+        }
+    }
+}
+
 // Per-slot destinations of one decoded codeword (null pointers: not wanted).
 struct SlotOut {
     uint8_t* packed;
@@ -339,7 +388,9 @@ struct SlotOut {
 // All iterations of one codeword group whose core LLRs are already in buf0
 // (Lold): cpb slots, this thread = sub-row s of slot `slot`; gllr = the
 // slot's codeword in global memory (suffix LLRs).  Ends with a barrier.
-template <bool WEIGHTED>
+// LAYERED: Lold is the one posterior buffer; early stop checks the syndrome
+// after each iteration in a separate pass.
+template <bool WEIGHTED, bool LAYERED>
 __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slot, uint32_t s,
                                           bool slot_done, float* buf0, uint8_t* hd0, float2* wpair,
                                           int* s_fail, uint4* st_base, const float* gllr, SlotOut out,
@@ -350,9 +401,9 @@ __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slo
     float* lnew = lold + static_cast<size_t>(cpb) * cf;   // accumulates the new posterior
     const uint8_t* hd = hd0 + static_cast<size_t>(slot) * tab.rows * z;
     const uint32_t s4old = smem_addr(lold) + 4u * s;
-    const uint32_t dnew = static_cast<uint32_t>(cpb) * static_cast<uint32_t>(cf) * 4u;
+    const uint32_t dnew = LAYERED ? 0u : static_cast<uint32_t>(cpb) * static_cast<uint32_t>(cf) * 4u;
     const uint32_t hd_base = smem_addr(hd) + s;
-    if (!slot_done)
+    if (!LAYERED && !slot_done)
         for (int k = static_cast<int>(s); k < cf / 4; k += z)
             reinterpret_cast<float4*>(lnew)[k] = reinterpret_cast<const float4*>(lold)[k];
     for (int t = 0; t < n_iter; t++) {
@@ -366,15 +417,34 @@ __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slo
         if (tid < cpb) s_fail[tid] = 0;
         __syncthreads();
         const bool act = !slot_done;
-        const bool check = early_stop && t > 0;
         const bool store = !last || out.app != nullptr;
+        if (LAYERED) {
+            const bool check = early_stop && !last;
+            iterate_rows<WEIGHTED, false, true>(tab, s, s4old, 0u, wpair, st_base, gllr, hd_base, nullptr, act,
+                                                first, store, early_stop || last, alpha);
+            if (check) {
+                if (act) check_rows(tab, s, s4old, hd_base, &s_fail[slot]);
+                __syncthreads();
+                const bool conv = act && s_fail[slot] == 0;
+                if (conv)  // HD of this iteration is a codeword
+                    write_outputs(tab, lold, hd, 1, st_base, s, out.packed, out.app, out.iters, t + 1, true);
+                slot_done = slot_done || conv;
+                if (__syncthreads_and(slot_done)) break;
+            }
+            if (last) {
+                if (!slot_done) write_outputs(tab, lold, hd, 1, st_base, s, out.packed, out.app, out.iters, n_iter, true);
+                break;
+            }
+            continue;
+        }
+        const bool check = early_stop && t > 0;
         const bool write_hd = check || last;
         float* app_cw = (check && out.app) ? out.app : nullptr;
         const uint32_t fail =
-            check ? iterate_rows<WEIGHTED, true>(tab, s, s4old, dnew, wpair, st_base, gllr, hd_base, app_cw,
-                                                act, first, store, write_hd, alpha)
-                  : iterate_rows<WEIGHTED, false>(tab, s, s4old, dnew, wpair, st_base, gllr, hd_base, app_cw,
-                                                 act, first, store, write_hd, alpha);
+            check ? iterate_rows<WEIGHTED, true, false>(tab, s, s4old, dnew, wpair, st_base, gllr, hd_base,
+                                                       app_cw, act, first, store, write_hd, alpha)
+                  : iterate_rows<WEIGHTED, false, false>(tab, s, s4old, dnew, wpair, st_base, gllr, hd_base,
+                                                        app_cw, act, first, store, write_hd, alpha);
         if (check) {
             if (act && fail) atomicOr(&s_fail[slot], 1);
             __syncthreads();
@@ -397,7 +467,7 @@ __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slo
 
 // MINB = CTAs per SM the register budget is sized for: 1 when shared memory
 // admits a single CTA per SM anyway (BG1 Z=384), 2 otherwise.
-template <bool WEIGHTED, int MINB>
+template <bool WEIGHTED, int MINB, bool LAYERED>
 __global__ void __launch_bounds__(kMaxThreads, MINB)
     decode_kernel(const __grid_constant__ CodeTable tab, const __grid_constant__ DecodeArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -448,7 +518,7 @@ __global__ void __launch_bounds__(kMaxThreads, MINB)
         const size_t cw = static_cast<size_t>(cw0 + (slot_done ? 0 : slot));
         SlotOut out{a.packed + cw * tab.packed_bytes, a.app ? a.app + cw * n : nullptr,
                     a.iters ? a.iters + cw : nullptr};
-        run_group<WEIGHTED>(tab, cpb, slot, s, slot_done, buf0, hd0, wpair, s_fail, st_base, a.llr + cw * n, out,
+        run_group<WEIGHTED, LAYERED>(tab, cpb, slot, s, slot_done, buf0, hd0, wpair, s_fail, st_base, a.llr + cw * n, out,
                             a.n_iter, a.early_stop, a.alpha, a.weights, a.n_w_iters);
     }
 }
@@ -510,7 +580,7 @@ __global__ void __launch_bounds__(kMaxThreads, 2)
         SlotOut out{a.packed + job.out_offset, nullptr, a.iters ? a.iters + jidx : nullptr};
         uint4* st_base = reinterpret_cast<uint4*>(a.state + static_cast<size_t>(blockIdx.x) * a.slot_words) +
                          static_cast<size_t>(valid_thread ? slot : 0) * tab.rows * z;
-        run_group<false>(tab, cpb, slot, s, !valid_thread, buf0, hd0, nullptr, s_fail, st_base,
+        run_group<false, false>(tab, cpb, slot, s, !valid_thread, buf0, hd0, nullptr, s_fail, st_base,
                          a.llr + job.llr_offset, out, a.n_iter, a.early_stop, a.alpha, nullptr, 1);
     }
 }
@@ -521,14 +591,18 @@ size_t decode_smem_bytes(const CodeTable& tab, int cpb) {
     return kHeaderBytes + static_cast<size_t>(kMaxEdges) * 8 + group_smem_bytes(tab, cpb);
 }
 
-template <bool W, int MINB>
+template <bool W, int MINB, bool LAY>
 const void* kernel_ptr() {
-    return reinterpret_cast<const void*>(&decode_kernel<W, MINB>);
+    return reinterpret_cast<const void*>(&decode_kernel<W, MINB, LAY>);
 }
 
-const void* select_kernel(bool weighted, int minb) {
-    if (weighted) return minb >= 2 ? kernel_ptr<true, 2>() : kernel_ptr<true, 1>();
-    return minb >= 2 ? kernel_ptr<false, 2>() : kernel_ptr<false, 1>();
+const void* select_kernel(bool weighted, int minb, bool layered) {
+    if (layered) {
+        if (weighted) return minb >= 2 ? kernel_ptr<true, 2, true>() : kernel_ptr<true, 1, true>();
+        return minb >= 2 ? kernel_ptr<false, 2, true>() : kernel_ptr<false, 1, true>();
+    }
+    if (weighted) return minb >= 2 ? kernel_ptr<true, 2, false>() : kernel_ptr<true, 1, false>();
+    return minb >= 2 ? kernel_ptr<false, 2, false>() : kernel_ptr<false, 1, false>();
 }
 
 cudaError_t launch_batch_decode(const BatchDecodeArgs& args, int grid, size_t smem, cudaStream_t stream) {
@@ -543,39 +617,35 @@ cudaError_t decode_kernel_attributes(size_t smem) {
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    for (int w = 0; w < 2; w++)
-        for (int m = 1; m <= 2; m++) {
-            cudaError_t e = cudaFuncSetAttribute(select_kernel(w != 0, m),
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 static_cast<int>(smem));
-            if (e != cudaSuccess) return e;
-        }
+    for (int l = 0; l < 2; l++)
+        for (int w = 0; w < 2; w++)
+            for (int m = 1; m <= 2; m++) {
+                cudaError_t e = cudaFuncSetAttribute(select_kernel(w != 0, m, l != 0),
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     static_cast<int>(smem));
+                if (e != cudaSuccess) return e;
+            }
     return cudaSuccess;
 }
 
 int decode_max_ctas_per_sm(bool weighted, int minb, int threads, size_t smem) {
-    int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, select_kernel(weighted, minb), threads,
-                                                      smem) != cudaSuccess)
-        return 0;
+    int n = 1 << 30;
+    for (int l = 0; l < 2; l++) {
+        int k = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, select_kernel(weighted, minb, l != 0), threads,
+                                                          smem) != cudaSuccess)
+            return 0;
+        n = k < n ? k : n;
+    }
     return n;
 }
 
 cudaError_t launch_decode(const CodeTable& tab, const DecodeArgs& args, int grid, int threads,
-                          size_t smem, bool weighted, int minb, cudaStream_t stream) {
+                          size_t smem, bool weighted, bool layered, int minb, cudaStream_t stream) {
     if (args.cpb < 1 || args.cpb > kMaxCpb) return cudaErrorInvalidValue;
-    if (weighted) {
-        if (minb >= 2)
-            decode_kernel<true, 2><<<grid, threads, smem, stream>>>(tab, args);
-        else
-            decode_kernel<true, 1><<<grid, threads, smem, stream>>>(tab, args);
-    } else {
-        if (minb >= 2)
-            decode_kernel<false, 2><<<grid, threads, smem, stream>>>(tab, args);
-        else
-            decode_kernel<false, 1><<<grid, threads, smem, stream>>>(tab, args);
-    }
-    return cudaGetLastError();
+    const void* k = select_kernel(weighted, minb, layered);
+    void* params[2] = {const_cast<CodeTable*>(&tab), const_cast<DecodeArgs*>(&args)};
+    return cudaLaunchKernel(k, dim3(grid), dim3(threads), params, smem, stream);
 }
 
 }  // namespace nrldpc

@@ -102,8 +102,9 @@ const void* batch_decode_kernel_ptr();
 
 // Host-side launchers (decode.cu / channel.cu).
 // minb: CTAs per SM the kernel's register budget assumes (1 or 2).
+// layered: row-sequential schedule (no reference counterpart) instead of flooding.
 cudaError_t launch_decode(const CodeTable& tab, const DecodeArgs& args, int grid, int threads,
-                          size_t smem, bool weighted, int minb, cudaStream_t stream);
+                          size_t smem, bool weighted, bool layered, int minb, cudaStream_t stream);
 size_t decode_smem_bytes(const CodeTable& tab, int cpb);
 cudaError_t decode_kernel_attributes(size_t smem);
 int decode_max_ctas_per_sm(bool weighted, int minb, int threads, size_t smem);
@@ -111,8 +112,8 @@ int decode_max_ctas_per_sm(bool weighted, int minb, int threads, size_t smem);
 // Learned weighted min-sum training kernels (wms.cu).
 size_t wms_smem_bytes(const CodeTable& tab, int cpb);
 cudaError_t wms_kernel_attributes(size_t smem);
-cudaError_t launch_wms(bool backward, const CodeTable& tab, const float* llr, const uint8_t* cw,
-                       const float* weights, uint4* states, float* gseed, uint4* gq, double* loss,
+cudaError_t launch_wms(bool backward, bool layered, const CodeTable& tab, const float* llr, const uint8_t* cw,
+                       const float* weights, uint4* states, float* gseed, uint4* gq, float* gh, double* loss,
                        double* grad, float* app, int* counters, int n_cw, int T, int cpb, int grid,
                        int threads, size_t smem, float scale, cudaStream_t stream);
 cudaError_t launch_adam(int n, float* w, const double* grad, float* m, float* v, int step, float lr,

@@ -17,6 +17,14 @@
 // feeds the argmin edge), so dloss/dQ of a row is two numbers; they are kept
 // per row between steps.  Gradients w.r.t. L are scattered with shared-memory
 // atomics (the order of these adds does not matter for a gradient).
+//
+// Layered schedule (no reference counterpart): rows in ascending order update
+// one posterior A in place, Q^t_e = A[col] - R^{t-1}_e, A[col] = Q^t_e + R^t_e.
+// Its adjoint walks iterations and rows in reverse with g = dloss/dA in
+// shared memory: dloss/dR^t_e = g[col] + h_e, dloss/dQ^t_e = g[col] + (argmin
+// terms), g[col] = dloss/dQ^t_e, and h_e = -dloss/dQ^t_e is carried to
+// iteration t-1 as the gradient of R^{t-1}_e (per lifted edge, in global
+// memory: it does not compress to two numbers per row).
 #include <cuda_runtime.h>
 
 #include "nrldpc_internal.h"
@@ -40,7 +48,7 @@ __device__ __forceinline__ float sigmoid_f(float z) { return 1.0f / (1.0f + expf
 __device__ __forceinline__ int cw_bit(const uint8_t* cw, int c) { return (cw[c >> 3] >> (c & 7)) & 1; }
 
 // ---- forward ------------------------------------------------------------------------
-template <int D>
+template <int D, bool LAYERED>
 __device__ __forceinline__ void fwd_row(const CodeTable& tab, int e0, uint32_t s, const float* lold,
                                         float* lnew, const float* w_prev, const float* w_cur,
                                         uint4 st, uint4* st_out) {
@@ -68,6 +76,7 @@ __device__ __forceinline__ void fwd_row(const CodeTable& tab, int e0, uint32_t s
         const uint32_t sb = (opar ^ (oq >> i)) & 1u;
         rold[i] = __uint_as_float(__float_as_uint(mag) | (sb << 31));
         const float q = __fsub_rn(lv[i], rold[i]);
+        if (LAYERED) rold[i] = q;  // the layered update needs Q, not R_old
         const float qa = fabsf(q);
         if (q < 0.0f) qmask |= 1u << i;
         const bool p1 = qa < m1, p2 = qa < m2;
@@ -80,24 +89,28 @@ __device__ __forceinline__ void fwd_row(const CodeTable& tab, int e0, uint32_t s
     const uint32_t par = static_cast<uint32_t>(__popc(qmask) & 1);
     float nv[D];
 #pragma unroll
-    for (int i = 0; i < D; i++) nv[i] = lnew[addr[i]];
+    for (int i = 0; i < D; i++) nv[i] = LAYERED ? 0.0f : lnew[addr[i]];
 #pragma unroll
     for (int i = 0; i < D; i++) {
         const float mag = __fmul_rn(w_cur[e0 + i], i == i1 ? m2 : m1);
         const uint32_t sb = (par ^ (qmask >> i)) & 1u;
         const float rn = __uint_as_float(__float_as_uint(mag) | (sb << 31));
-        lnew[addr[i]] = __fadd_rn(nv[i], __fsub_rn(rn, rold[i]));
+        if (LAYERED)
+            lnew[addr[i]] = __fadd_rn(rold[i], rn);  // A = Q + R_new
+        else
+            lnew[addr[i]] = __fadd_rn(nv[i], __fsub_rn(rn, rold[i]));
     }
     *st_out = make_uint4(__float_as_uint(m1), __float_as_uint(m2),
                          static_cast<uint32_t>(i1) | (qmask << 8), static_cast<uint32_t>(i2));
 }
 
+template <bool LAYERED>
 __device__ __forceinline__ void fwd_dispatch(int deg, const CodeTable& tab, int e0, uint32_t s,
                                              const float* lold, float* lnew, const float* wp,
                                              const float* wc, uint4 st, uint4* st_out) {
     switch (deg) {
 #define NRLDPC_FWD_CASE(D) \
-    case D: fwd_row<D>(tab, e0, s, lold, lnew, wp, wc, st, st_out); break;
+    case D: fwd_row<D, LAYERED>(tab, e0, s, lold, lnew, wp, wc, st, st_out); break;
         NRLDPC_FWD_CASE(1) NRLDPC_FWD_CASE(2) NRLDPC_FWD_CASE(3) NRLDPC_FWD_CASE(4)
         NRLDPC_FWD_CASE(5) NRLDPC_FWD_CASE(6) NRLDPC_FWD_CASE(7) NRLDPC_FWD_CASE(8)
         NRLDPC_FWD_CASE(9) NRLDPC_FWD_CASE(10) NRLDPC_FWD_CASE(11) NRLDPC_FWD_CASE(12)
@@ -114,7 +127,8 @@ struct WmsArgs {
     const float* weights;    // [T][E]
     uint4* states;           // [T][n_cw][rows*Z]
     float* gseed;            // [T][n_cw][n_bp]
-    uint4* gq;               // [grid*cpb][rows*Z] adjoint per-row dloss/dQ (backward)
+    uint4* gq;               // [grid*cpb][rows*Z] adjoint per-row dloss/dQ (flooding backward)
+    float* gh;               // [grid*cpb][E*Z] adjoint per-edge dloss/dR (layered backward)
     double* loss;            // forward: += loss
     double* grad;            // backward: += dloss/dw [T][E]
     float* app;              // optional L^T
@@ -124,6 +138,7 @@ struct WmsArgs {
     float scale;
 };
 
+template <bool LAYERED>
 __global__ void __launch_bounds__(kMaxThreads, 1)
     wms_forward_kernel(const __grid_constant__ CodeTable tab, const __grid_constant__ WmsArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -143,7 +158,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
         const int cw = g * cpb + slot;
         const bool act = valid && cw < a.n_cw;
         float* lold = bufs + static_cast<size_t>(slot) * n;
-        float* lnew = bufs + static_cast<size_t>(cpb + slot) * n;
+        float* lnew = LAYERED ? lold : bufs + static_cast<size_t>(cpb + slot) * n;
         if (act) {
             const float4* src = reinterpret_cast<const float4*>(a.llr + static_cast<size_t>(cw) * n);
             for (int k = static_cast<int>(s); k < n / 4; k += z) reinterpret_cast<float4*>(lold)[k] = src[k];
@@ -155,7 +170,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
                 wbuf[kMaxEdges + e] = a.weights[t * E + e];
             }
             __syncthreads();
-            if (act)
+            if (act && !LAYERED)
                 for (int k = static_cast<int>(s); k < n / 4; k += z)
                     reinterpret_cast<float4*>(lnew)[k] = reinterpret_cast<const float4*>(lold)[k];
             __syncthreads();
@@ -167,7 +182,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
                 if (act) {
                     uint4 st = make_uint4(0u, 0u, 0u, 0u);
                     if (t > 0) st = __ldcg(st_prev + r * z + s);
-                    fwd_dispatch(tab.row_deg[r], tab, tab.row_ptr[r], s, lold, lnew, wbuf,
+                    fwd_dispatch<LAYERED>(tab.row_deg[r], tab, tab.row_ptr[r], s, lold, lnew, wbuf,
                                  wbuf + kMaxEdges, st, st_cur + r * z + s);
                 }
                 if (tab.sync_after[r]) __syncthreads();
@@ -319,6 +334,115 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
     }
 }
 
+template <int D>
+__device__ __forceinline__ void bwd_layered_row(const CodeTable& tab, int e0, uint32_t s, bool act, float* g,
+                                                const float* w_cur, float* gw_acc, uint4 st, float* gh_row,
+                                                bool has_h, bool write_h) {
+    const uint32_t z = static_cast<uint32_t>(tab.z);
+    const float m1 = __uint_as_float(st.x), m2 = __uint_as_float(st.y);
+    const int i1 = static_cast<int>(st.z & 31u), i2 = static_cast<int>(st.w);
+    const uint32_t q = st.z >> 8;
+    const uint32_t par = static_cast<uint32_t>(__popc(q) & 1);
+    uint32_t ad[D];
+    float ga[D];
+    float to1 = 0.0f, to2 = 0.0f;  // dloss/dQ at the argmin edges through R
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+        const uint32_t ed = tab.edge[e0 + i];
+        uint32_t a = s + (ed & 0xffffu);
+        if (s >= (ed >> 16)) a -= z;
+        ad[i] = a;
+        float dr = 0.0f;
+        ga[i] = 0.0f;
+        if (act) {
+            ga[i] = g[a];
+            dr = ga[i] + (has_h ? gh_row[i * z] : 0.0f);
+        }
+        const float sg = ((par ^ (q >> i)) & 1u) ? -1.0f : 1.0f;
+        const float mag = i == i1 ? m2 : m1;
+        float gw = act ? dr * sg * mag : 0.0f;
+        for (int off = 16; off > 0; off >>= 1) gw += __shfl_xor_sync(0xffffffffu, gw, off);
+        if ((threadIdx.x & 31) == 0) atomicAdd(&gw_acc[e0 + i], gw);
+        const float t = dr * w_cur[e0 + i] * sg;
+        if (i == i1) to2 = t;
+        else to1 += t;
+    }
+    if (!act) return;
+    const float g1 = m1 < 1000.0f ? to1 * (((q >> i1) & 1u) ? -1.0f : 1.0f) : 0.0f;
+    const float g2 = (i2 < D && m2 < 1000.0f) ? to2 * (((q >> i2) & 1u) ? -1.0f : 1.0f) : 0.0f;
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+        float dq = ga[i];
+        if (i == i1) dq += g1;
+        if (i == i2) dq += g2;
+        if (i == i1 || i == i2) g[ad[i]] = dq;  // dloss/dA before this row
+        if (write_h) gh_row[i * z] = -dq;      // dloss/dR^{t-1}
+    }
+}
+
+__device__ __forceinline__ void bwd_layered_dispatch(int deg, const CodeTable& tab, int e0, uint32_t s, bool act,
+                                                     float* g, const float* wc, float* gw_acc, uint4 st,
+                                                     float* gh_row, bool has_h, bool write_h) {
+    switch (deg) {
+#define NRLDPC_BWDL_CASE(D) \
+    case D: bwd_layered_row<D>(tab, e0, s, act, g, wc, gw_acc, st, gh_row, has_h, write_h); break;
+        NRLDPC_BWDL_CASE(1) NRLDPC_BWDL_CASE(2) NRLDPC_BWDL_CASE(3) NRLDPC_BWDL_CASE(4)
+        NRLDPC_BWDL_CASE(5) NRLDPC_BWDL_CASE(6) NRLDPC_BWDL_CASE(7) NRLDPC_BWDL_CASE(8)
+        NRLDPC_BWDL_CASE(9) NRLDPC_BWDL_CASE(10) NRLDPC_BWDL_CASE(11) NRLDPC_BWDL_CASE(12)
+        NRLDPC_BWDL_CASE(13) NRLDPC_BWDL_CASE(14) NRLDPC_BWDL_CASE(15) NRLDPC_BWDL_CASE(16)
+        NRLDPC_BWDL_CASE(17) NRLDPC_BWDL_CASE(18) NRLDPC_BWDL_CASE(19)
+#undef NRLDPC_BWDL_CASE
+        default: break;
+    }
+}
+
+__global__ void __launch_bounds__(kMaxThreads, 1)
+    wms_backward_layered_kernel(const __grid_constant__ CodeTable tab, const __grid_constant__ WmsArgs a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    int* s_group = reinterpret_cast<int*>(smem);
+    float* wcur = reinterpret_cast<float*>(smem + kHdr);  // [E]
+    float* gw_acc = wcur + kMaxEdges;                     // [E]
+    float* bufs = gw_acc + kMaxEdges;
+    const int z = tab.z, n = tab.n_bp, cpb = a.cpb, rows = tab.rows, E = tab.n_edges;
+    const int tid = threadIdx.x, slot = tid / z;
+    const uint32_t s = static_cast<uint32_t>(tid - slot * z);
+    const bool valid = slot < cpb;
+    float* gh = a.gh + (static_cast<size_t>(blockIdx.x) * cpb + (valid ? slot : 0)) * E * z;
+    for (;;) {
+        if (tid == 0) *s_group = atomicAdd(a.work_counter, 1);
+        __syncthreads();
+        const int grp = *s_group;
+        if (grp >= a.n_groups) break;
+        const int cw = grp * cpb + slot;
+        const bool act = valid && cw < a.n_cw;
+        float* g = bufs + static_cast<size_t>(valid ? slot : 0) * n;  // dloss/dA
+        if (act)
+            for (int c = static_cast<int>(s); c < n; c += z) g[c] = 0.0f;
+        for (int t = a.T - 1; t >= 0; t--) {
+            for (int e = tid; e < E; e += blockDim.x) {
+                wcur[e] = a.weights[t * E + e];
+                gw_acc[e] = 0.0f;
+            }
+            if (act) {
+                const float* seed = a.gseed + (static_cast<size_t>(t) * a.n_cw + cw) * n;
+                for (int c = static_cast<int>(s); c < n; c += z) g[c] += seed[c];
+            }
+            __syncthreads();
+            const uint4* st = a.states + (static_cast<size_t>(t) * a.n_cw + (act ? cw : 0)) * rows * z;
+            for (int r = rows - 1; r >= 0; r--) {
+                const uint4 sv = act ? __ldcg(st + r * z + s) : make_uint4(0u, 0u, 0u, 31u);
+                bwd_layered_dispatch(tab.row_deg[r], tab, tab.row_ptr[r], s, act, g, wcur, gw_acc, sv,
+                                     gh + static_cast<size_t>(tab.row_ptr[r]) * z + s, t < a.T - 1, t > 0);
+                if (r > 0 && tab.sync_after[r - 1]) __syncthreads();
+            }
+            __syncthreads();
+            for (int e = tid; e < E; e += blockDim.x)
+                if (gw_acc[e] != 0.0f) atomicAdd(&a.grad[t * E + e], static_cast<double>(gw_acc[e]));
+            __syncthreads();
+        }
+    }
+}
+
 __global__ void adam_kernel(int n, float* w, const double* grad, float* m, float* v, float lr,
                             float b1, float b2, float eps, float c1, float c2, float w_min) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -339,16 +463,20 @@ size_t wms_smem_bytes(const CodeTable& tab, int cpb) {
 }
 
 cudaError_t wms_kernel_attributes(size_t smem) {
-    cudaError_t e = cudaFuncSetAttribute(reinterpret_cast<const void*>(&wms_forward_kernel),
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem));
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(reinterpret_cast<const void*>(&wms_backward_kernel),
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    const void* ks[4] = {reinterpret_cast<const void*>(&wms_forward_kernel<false>),
+                         reinterpret_cast<const void*>(&wms_forward_kernel<true>),
+                         reinterpret_cast<const void*>(&wms_backward_kernel),
+                         reinterpret_cast<const void*>(&wms_backward_layered_kernel)};
+    for (const void* k : ks) {
+        cudaError_t e =
+            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
-cudaError_t launch_wms(bool backward, const CodeTable& tab, const float* llr, const uint8_t* cw,
-                       const float* weights, uint4* states, float* gseed, uint4* gq, double* loss,
+cudaError_t launch_wms(bool backward, bool layered, const CodeTable& tab, const float* llr, const uint8_t* cw,
+                       const float* weights, uint4* states, float* gseed, uint4* gq, float* gh, double* loss,
                        double* grad, float* app, int* counters, int n_cw, int T, int cpb, int grid,
                        int threads, size_t smem, float scale, cudaStream_t stream) {
     WmsArgs a{};
@@ -358,6 +486,7 @@ cudaError_t launch_wms(bool backward, const CodeTable& tab, const float* llr, co
     a.states = states;
     a.gseed = gseed;
     a.gq = gq;
+    a.gh = gh;
     a.loss = loss;
     a.grad = grad;
     a.app = app;
@@ -369,10 +498,14 @@ cudaError_t launch_wms(bool backward, const CodeTable& tab, const float* llr, co
     a.n_groups = (n_cw + cpb - 1) / cpb;
     a.scale = scale;
     grid = grid < a.n_groups ? grid : a.n_groups;
-    if (backward)
+    if (backward && layered)
+        wms_backward_layered_kernel<<<grid, threads, smem, stream>>>(tab, a);
+    else if (backward)
         wms_backward_kernel<<<grid, threads, smem, stream>>>(tab, a);
+    else if (layered)
+        wms_forward_kernel<true><<<grid, threads, smem, stream>>>(tab, a);
     else
-        wms_forward_kernel<<<grid, threads, smem, stream>>>(tab, a);
+        wms_forward_kernel<false><<<grid, threads, smem, stream>>>(tab, a);
     return cudaGetLastError();
 }
 

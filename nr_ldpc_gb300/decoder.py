@@ -61,6 +61,7 @@ class Decoder:
         _lib.check("nrldpc_geometry", lib.nrldpc_geometry(h, *[C.byref(v) for v in vals]))
         self.rows, self.cols, _, self.n_edges, self.n_bp, self.packed_bytes = [v.value for v in vals]
         self.n_info = self.kb * self.z
+        self.schedule = "flooding"
 
     def close(self):
         if getattr(self, "_h", None):
@@ -132,6 +133,16 @@ class Decoder:
                                                         float(scale), C.c_void_p(packed_host.data_ptr()),
                                                         n, int(n_iter), int(bool(early_stop)),
                                                         _stream_ptr(stream)))
+
+    # ---- schedule -------------------------------------------------------------------
+    FLOODING, LAYERED = 0, 1
+
+    def set_schedule(self, schedule) -> None:
+        """'flooding' (the reference's, default) or 'layered' (row-sequential,
+        in-place posterior; no reference counterpart)."""
+        code = {"flooding": 0, "layered": 1}.get(schedule, schedule)
+        _lib.check("nrldpc_set_schedule", self._lib.nrldpc_set_schedule(self._h, int(code)))
+        self.schedule = "layered" if code == 1 else "flooding"
 
     # ---- learned weights ------------------------------------------------------------
     def set_weights(self, w) -> None:

@@ -31,12 +31,15 @@ def sigma_from_ebn0(ebn0_db: torch.Tensor, rate: float) -> torch.Tensor:
 
 
 class Trainer:
-    """Trains w[n_iter][n_edges] for one base graph at one lifting size."""
+    """Trains w[n_iter][n_edges] for one base graph at one lifting size,
+    under the flooding (the reference's) or the layered schedule."""
 
     def __init__(self, bg: int = 2, z: int = 128, n_iter: int = 8, batch: int = 16384,
                  chunk: int = 4096, lr: float = 1e-3, ebn0_range=(1.0, 3.0), w_init: float = 0.75,
-                 seed: int = 1, device: int = 0):
+                 seed: int = 1, device: int = 0, schedule: str = "flooding"):
         self.dec = Decoder(bg=bg, z=z, max_batch=chunk, device=device)
+        self.dec.set_schedule(schedule)
+        self.schedule = schedule
         self.lib = _lib.load()
         self.bg, self.z, self.T, self.batch, self.chunk = bg, z, n_iter, batch, chunk
         self.lr, self.ebn0_range, self.seed = lr, ebn0_range, seed
@@ -115,7 +118,7 @@ class Trainer:
 
     def save(self, path: str, meta: Optional[dict] = None):
         np.save(path + ".npy", self.weights())
-        info = dict(bg=self.bg, z=self.z, n_iter=self.T, batch=self.batch, lr=self.lr,
+        info = dict(bg=self.bg, z=self.z, n_iter=self.T, batch=self.batch, lr=self.lr, schedule=self.schedule,
                     ebn0_range=list(self.ebn0_range), seed=self.seed, steps=self.step_count)
         info.update(meta or {})
         with open(path + ".json", "w") as f:

@@ -6,7 +6,8 @@
 Defaults follow the training configuration the project is specified on:
 8 unrolled iterations, weights initialised to 0.75, 16384 seeded codewords
 per step at Eb/N0 uniform in [1, 3] dB, BCE on the posterior LLRs, Adam with
-learning rate 1e-3.
+learning rate 1e-3.  --schedule layered trains the row-sequential decoder
+(its own forward and adjoint kernels) instead of the flooding one.
 """
 from __future__ import annotations
 
@@ -27,10 +28,11 @@ def main():
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--ebn0", type=float, nargs=2, default=[1.0, 3.0])
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--schedule", default="flooding", choices=["flooding", "layered"])
     ap.add_argument("--out", required=True)
     args = ap.parse_args()
     tr = Trainer(bg=args.bg, z=args.z, n_iter=args.iters, batch=args.batch, chunk=args.chunk,
-                 lr=args.lr, ebn0_range=tuple(args.ebn0), seed=args.seed)
+                 lr=args.lr, ebn0_range=tuple(args.ebn0), seed=args.seed, schedule=args.schedule)
     t0 = time.time()
     hist = tr.train(args.steps, log_every=max(1, args.steps // 20))
     dt = time.time() - t0

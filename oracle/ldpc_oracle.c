@@ -190,8 +190,12 @@ static void decode_one_f32(const orc_code* c, const float* llr, int n_iter, floa
 typedef struct {
     const orc_code* c; const float* llr; int n_iter; float alpha; const float* w; int n_w;
     int early; uint8_t* packed; float* app; int32_t* iters;
-    int cw_begin, cw_end;
+    int cw_begin, cw_end, layered;
 } job_f32;
+
+static void decode_one_layered_f32(const orc_code* c, const float* llr, int n_iter, float alpha,
+                                   const float* w, int n_w_iters, int early, ws_f32* ws,
+                                   uint8_t* packed, float* app, int32_t* iters);
 
 static void* run_job_f32(void* arg) {
     job_f32* j = (job_f32*)arg;
@@ -203,16 +207,17 @@ static void* run_job_f32(void* arg) {
     ws.dt = (float*)malloc(sizeof(float) * EZ);
     ws.hd = (uint8_t*)malloc(N);
     for (int i = j->cw_begin; i < j->cw_end; i++)
-        decode_one_f32(c, j->llr + (size_t)i * N, j->n_iter, j->alpha, j->w, j->n_w, j->early, &ws,
-                       j->packed + (size_t)i * PACKED_BYTES(N), j->app ? j->app + (size_t)i * N : NULL,
-                       j->iters ? j->iters + i : NULL);
+        (j->layered ? decode_one_layered_f32 : decode_one_f32)(
+            c, j->llr + (size_t)i * N, j->n_iter, j->alpha, j->w, j->n_w, j->early, &ws,
+            j->packed + (size_t)i * PACKED_BYTES(N), j->app ? j->app + (size_t)i * N : NULL,
+            j->iters ? j->iters + i : NULL);
     free(ws.L); free(ws.R); free(ws.dt); free(ws.hd);
     return NULL;
 }
 
 static int decode_f32_common(const orc_code* c, const float* llr, int n_cw, int n_iter,
                              float alpha, const float* w, int n_w, int early, uint8_t* packed,
-                             float* app, int32_t* iters, int n_threads) {
+                             float* app, int32_t* iters, int n_threads, int layered) {
     if (!c || !llr || !packed || n_cw < 0 || n_iter < 1) return -1;
     if (n_threads < 1) n_threads = 1;
     if (n_threads > n_cw) n_threads = n_cw > 0 ? n_cw : 1;
@@ -221,7 +226,8 @@ static int decode_f32_common(const orc_code* c, const float* llr, int n_cw, int 
     if (n_threads > 256) n_threads = 256;
     for (int k = 0; k < n_threads; k++) {
         jobs[k] = (job_f32){c, llr, n_iter, alpha, w, n_w, early, packed, app, iters,
-                            (int)((long)n_cw * k / n_threads), (int)((long)n_cw * (k + 1) / n_threads)};
+                            (int)((long)n_cw * k / n_threads), (int)((long)n_cw * (k + 1) / n_threads),
+                            layered};
     }
     if (n_threads == 1) { run_job_f32(&jobs[0]); return 0; }
     for (int k = 0; k < n_threads; k++) pthread_create(&th[k], NULL, run_job_f32, &jobs[k]);
@@ -232,7 +238,7 @@ static int decode_f32_common(const orc_code* c, const float* llr, int n_cw, int 
 int orc_minsum_f32(const orc_code* c, const float* llr, int n_cw, int n_iter, float alpha,
                    int early_stop, uint8_t* packed, float* app, int32_t* iters, int n_threads) {
     return decode_f32_common(c, llr, n_cw, n_iter, alpha, NULL, 0, early_stop, packed, app, iters,
-                             n_threads);
+                             n_threads, 0);
 }
 
 int orc_wms_decode_f32(const orc_code* c, const float* llr, int n_cw, int n_iter, const float* w,
@@ -240,7 +246,71 @@ int orc_wms_decode_f32(const orc_code* c, const float* llr, int n_cw, int n_iter
                        int32_t* iters) {
     if (!w || n_weight_iters < 1) return -1;
     return decode_f32_common(c, llr, n_cw, n_iter, 0.0f, w, n_weight_iters, early_stop, packed, app,
-                             iters, 1);
+                             iters, 1, 0);
+}
+
+int orc_layered_f32(const orc_code* c, const float* llr, int n_cw, int n_iter, float alpha,
+                    const float* w, int n_weight_iters, int early_stop, uint8_t* packed, float* app,
+                    int32_t* iters, int n_threads) {
+    if (w && n_weight_iters < 1) return -1;
+    return decode_f32_common(c, llr, n_cw, n_iter, alpha, w, w ? n_weight_iters : 0, early_stop, packed,
+                             app, iters, n_threads, 1);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Layered (row-sequential) schedule, fp32.  No reference counterpart: the
+ * reference decodes with the flooding schedule only.  Same check-node rules
+ * as decode_one_f32 (strict '<' from 1000.0f, first argmin, R = +-fl(a*min));
+ * rows run in ascending order and each updates the posterior in place:
+ *   Q_e = A[col] - R_old_e;  A[col] = Q_e + R_new_e.
+ * early: after iteration t < n_iter - 1, stop when the syndrome of HD(A) is
+ * zero (iters = t + 1). */
+static void decode_one_layered_f32(const orc_code* c, const float* llr, int n_iter, float alpha,
+                                   const float* w, int n_w_iters, int early, ws_f32* ws,
+                                   uint8_t* packed, float* app, int32_t* iters) {
+    const int z = c->z, N = c->cols * z;
+    float* A = ws->L; float* R = ws->R; float* Q = ws->dt; uint8_t* hd = ws->hd;
+    memcpy(A, llr, sizeof(float) * N);
+    memset(R, 0, sizeof(float) * (size_t)c->n_edges * z);
+    int t_done = n_iter;
+    for (int t = 0; t < n_iter; t++) {
+        for (int r = 0; r < c->rows; r++) {
+            const int e0 = c->row_ptr[r], deg = c->row_ptr[r + 1] - e0;
+            for (int s = 0; s < z; s++) {
+                int q_sign = 0, idx_min = 0;
+                float sign = 1.0f, rmin1 = 1000.0f, rmin2 = 1000.0f;
+                for (int i = 0; i < deg; i++) {
+                    const int e = e0 + i;
+                    const float q = A[edge_col(c, e, s)] - R[e * z + s];
+                    Q[e * z + s] = q;
+                    const float q_abs = fabsf(q);
+                    const int sq = q < 0.0f;
+                    sign = sign * (float)(1 - sq * 2);
+                    q_sign |= sq << i;
+                    if (q_abs < rmin1) {
+                        rmin2 = rmin1; rmin1 = q_abs; idx_min = i;
+                    } else if (q_abs < rmin2) {
+                        rmin2 = q_abs;
+                    }
+                }
+                for (int i = 0; i < deg; i++) {
+                    const int e = e0 + i;
+                    const float sq = (float)(1 - 2 * ((q_sign >> i) & 1));
+                    const float a = w ? w[(t < n_w_iters ? t : n_w_iters - 1) * c->n_edges + e] : alpha;
+                    float r_new = a * sign;
+                    r_new = r_new * sq;
+                    r_new = r_new * (i != idx_min ? rmin1 : rmin2);
+                    R[e * z + s] = r_new;
+                    A[edge_col(c, e, s)] = Q[e * z + s] + r_new;
+                }
+            }
+        }
+        for (int i = 0; i < N; i++) hd[i] = (A[i] > 0.0f) ? 0 : 1;
+        if (early && t < n_iter - 1 && syndrome_weight_hd(c, hd) == 0) { t_done = t + 1; break; }
+    }
+    pack_hd(hd, N, packed);
+    if (app) memcpy(app, A, sizeof(float) * N);
+    if (iters) *iters = t_done;
 }
 
 /* ------------------------------------------------------------------------- */
@@ -725,5 +795,111 @@ double orc_wms_loss_grad_f64(const orc_code* c, const float* llr, const uint8_t*
         }
     }
     free(Q); free(Lh); free(R); free(Rn); free(gL); free(gQn); free(gQ);
+    return loss;
+}
+
+/* Layered weighted min-sum: forward + adjoint in double precision.  No
+ * reference counterpart.  Forward per iteration t, rows ascending:
+ *   Q^t_e = A[col] - R^{t-1}_e;  R^t_e = w[t][e] * sign_e * min_e;
+ *   A[col] = Q^t_e + R^t_e;  loss += scale * sum_c softplus(-y_c A_c) after t.
+ * Adjoint, t = T-1 .. 0, rows descending, with g = dloss/dA and
+ * h_e = dloss/dR^t_e from iteration t+1 (Q^{t+1}_e = A - R^t_e):
+ *   dR_e = g[col] + h_e;  dQ_e = g[col] + (argmin terms);  g[col] = dQ_e;
+ *   h_e <- -dQ_e for iteration t-1. */
+double orc_wms_layered_loss_grad_f64(const orc_code* c, const float* llr, const uint8_t* cw_packed,
+                                     int n_cw, int n_iter, const double* w, double* grad, double* app) {
+    const int z = c->z, N = c->cols * z, E = c->n_edges, EZ = E * z, T = n_iter;
+    double* Qs = (double*)malloc(sizeof(double) * (size_t)T * EZ); /* Q^t per edge */
+    double* Ah = (double*)malloc(sizeof(double) * (size_t)T * N);  /* A after iteration t */
+    double* A = (double*)malloc(sizeof(double) * N);
+    double* R = (double*)malloc(sizeof(double) * EZ);
+    double* g = (double*)malloc(sizeof(double) * N);
+    double* h = (double*)malloc(sizeof(double) * EZ);
+    double* dR = (double*)malloc(sizeof(double) * 32);
+    const double scale = 1.0 / ((double)T * n_cw * N);
+    double loss = 0.0;
+    if (grad) memset(grad, 0, sizeof(double) * T * E);
+    for (int cw = 0; cw < n_cw; cw++) {
+        const uint8_t* bits = cw_packed + (size_t)cw * PACKED_BYTES(N);
+        for (int i = 0; i < N; i++) A[i] = llr[(size_t)cw * N + i];
+        memset(R, 0, sizeof(double) * EZ);
+        for (int t = 0; t < T; t++) {
+            double* Qt = Qs + (size_t)t * EZ;
+            for (int r = 0; r < c->rows; r++) {
+                const int e0 = c->row_ptr[r], deg = c->row_ptr[r + 1] - e0;
+                for (int s = 0; s < z; s++) {
+                    int q_sign = 0, i1 = 0;
+                    double m1 = 1000.0, m2 = 1000.0;
+                    for (int i = 0; i < deg; i++) {
+                        const int e = e0 + i;
+                        const double q = A[edge_col(c, e, s)] - R[e * z + s];
+                        Qt[e * z + s] = q;
+                        const double qa = fabs(q);
+                        q_sign ^= (q < 0) << i;
+                        if (qa < m1) { m2 = m1; m1 = qa; i1 = i; } else if (qa < m2) m2 = qa;
+                    }
+                    const int par = __builtin_popcount(q_sign) & 1;
+                    for (int i = 0; i < deg; i++) {
+                        const int e = e0 + i;
+                        const int sb = par ^ ((q_sign >> i) & 1);
+                        const double mag = i != i1 ? m1 : m2;
+                        R[e * z + s] = w[t * E + e] * (sb ? -mag : mag);
+                        A[edge_col(c, e, s)] = Qt[e * z + s] + R[e * z + s];
+                    }
+                }
+            }
+            memcpy(Ah + (size_t)t * N, A, sizeof(double) * N);
+            for (int i = 0; i < N; i++) {
+                const double y = ((bits[i >> 3] >> (i & 7)) & 1) ? -1.0 : 1.0;
+                loss += scale * softplus(-y * A[i]);
+            }
+        }
+        if (app) memcpy(app + (size_t)cw * N, A, sizeof(double) * N);
+        if (!grad) continue;
+        memset(g, 0, sizeof(double) * N);
+        memset(h, 0, sizeof(double) * EZ);
+        for (int t = T - 1; t >= 0; t--) {
+            const double* At = Ah + (size_t)t * N;
+            for (int i = 0; i < N; i++) {
+                const double y = ((bits[i >> 3] >> (i & 7)) & 1) ? -1.0 : 1.0;
+                g[i] += scale * (-y) * sigm(-y * At[i]);
+            }
+            const double* Qt = Qs + (size_t)t * EZ;
+            for (int r = c->rows - 1; r >= 0; r--) {
+                const int e0 = c->row_ptr[r], deg = c->row_ptr[r + 1] - e0;
+                for (int s = 0; s < z; s++) {
+                    int q_sign = 0, i1 = -1, i2 = -1;
+                    double m1 = 1000.0, m2 = 1000.0;
+                    for (int i = 0; i < deg; i++) {
+                        const double qa = fabs(Qt[(e0 + i) * z + s]);
+                        q_sign ^= (Qt[(e0 + i) * z + s] < 0) << i;
+                        if (qa < m1) { m2 = m1; i2 = i1; m1 = qa; i1 = i; }
+                        else if (qa < m2) { m2 = qa; i2 = i; }
+                    }
+                    const int par = __builtin_popcount(q_sign) & 1;
+                    double to1 = 0.0, to2 = 0.0; /* dloss/dQ at the argmin edges via R */
+                    for (int i = 0; i < deg; i++) {
+                        const int e = e0 + i;
+                        dR[i] = g[edge_col(c, e, s)] + h[e * z + s];
+                        const double sgn = (par ^ ((q_sign >> i) & 1)) ? -1.0 : 1.0;
+                        grad[t * E + e] += dR[i] * sgn * (i != i1 ? m1 : m2);
+                        const double term = dR[i] * w[t * E + e] * sgn;
+                        if (i != i1) to1 += term; else to2 += term;
+                    }
+                    for (int i = 0; i < deg; i++) {
+                        const int e = e0 + i;
+                        const int col = edge_col(c, e, s);
+                        double dq = g[col];
+                        const double sq = Qt[e * z + s] < 0 ? -1.0 : 1.0;
+                        if (i == i1 && i1 >= 0) dq += to1 * sq;
+                        if (i == i2 && i2 >= 0) dq += to2 * sq;
+                        g[col] = dq;
+                        h[e * z + s] = -dq;
+                    }
+                }
+            }
+        }
+    }
+    free(Qs); free(Ah); free(A); free(R); free(g); free(h); free(dR);
     return loss;
 }

@@ -117,6 +117,22 @@ int orc_wms_decode_f32(const orc_code* c, const float* llr, int n_cw, int n_iter
                        const float* w, int n_weight_iters, int early_stop, uint8_t* packed,
                        float* app, int32_t* iters);
 
+/* Layered (row-sequential) normalized or weighted min-sum, fp32.  No
+ * reference counterpart (the reference's schedule is flooding).  Rows in
+ * ascending order update the posterior in place: Q = A - R_old,
+ * A = Q + R_new; check-node rules as orc_minsum_f32.  w == NULL -> alpha,
+ * else weights [n_weight_iters][E] (t >= n_weight_iters reuse the last row).
+ * early_stop: stop after iteration t when the syndrome of HD_t is zero
+ * (iters = t + 1). */
+int orc_layered_f32(const orc_code* c, const float* llr, int n_cw, int n_iter, float alpha,
+                    const float* w, int n_weight_iters, int early_stop, uint8_t* packed, float* app,
+                    int32_t* iters, int n_threads);
+
+/* Loss and gradient of the layered weighted min-sum (double precision; same
+ * loss as orc_wms_loss_grad_f64, posterior updated row by row in place). */
+double orc_wms_layered_loss_grad_f64(const orc_code* c, const float* llr, const uint8_t* cw_packed,
+                                     int n_cw, int n_iter, const double* w, double* grad, double* app);
+
 #ifdef __cplusplus
 }
 #endif

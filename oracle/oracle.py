@@ -59,8 +59,13 @@ def lib():
         L.orc_wms_loss_grad_f64.restype = C.c_double
         L.orc_wms_loss_grad_f64.argtypes = [C.c_void_p, _f32p, _u8p, C.c_int, C.c_int, _f64p,
                                             C.c_void_p, C.c_void_p]
+        L.orc_wms_layered_loss_grad_f64.restype = C.c_double
+        L.orc_wms_layered_loss_grad_f64.argtypes = [C.c_void_p, _f32p, _u8p, C.c_int, C.c_int, _f64p,
+                                                    C.c_void_p, C.c_void_p]
         L.orc_wms_decode_f32.argtypes = [C.c_void_p, _f32p, C.c_int, C.c_int, _f32p, C.c_int,
                                          C.c_int, _u8p, C.c_void_p, C.c_void_p]
+        L.orc_layered_f32.argtypes = [C.c_void_p, _f32p, C.c_int, C.c_int, C.c_float, C.c_void_p,
+                                      C.c_int, C.c_int, _u8p, C.c_void_p, C.c_void_p, C.c_int]
         L.orc_crc.restype = C.c_uint32
         L.orc_crc.argtypes = [_u8p, C.c_int, C.c_uint32, C.c_int]
         L.orc_rm_k0.argtypes = [C.c_int, C.c_int, C.c_int]
@@ -109,6 +114,21 @@ class OracleCode:
             raise RuntimeError(f"orc_minsum_f32 rc={rc}")
         return packed, app, iters
 
+    def layered_f32(self, llr, n_iter, alpha=0.75, w=None, early_stop=False, want_app=False, threads=1):
+        """Layered-schedule min-sum (w: [T, E] weights or None for alpha)."""
+        llr = np.ascontiguousarray(llr, dtype=np.float32).reshape(-1, self.n_bp)
+        n = llr.shape[0]
+        packed = np.zeros((n, self.n_bytes), np.uint8)
+        app = np.zeros((n, self.n_bp), np.float32) if want_app else None
+        iters = np.zeros(n, np.int32)
+        wa = None if w is None else np.ascontiguousarray(w, dtype=np.float32)
+        rc = lib().orc_layered_f32(self._h, llr, n, int(n_iter), float(alpha), _ptr(wa),
+                                   0 if wa is None else wa.shape[0], int(early_stop), packed, _ptr(app),
+                                   _ptr(iters), int(threads))
+        if rc:
+            raise RuntimeError(f"orc_layered_f32 rc={rc}")
+        return packed, app, iters
+
     def minsum_f64(self, llr, n_iter, alpha=0.75, early_stop=False):
         llr = np.ascontiguousarray(llr, dtype=np.float64).reshape(-1, self.n_bp)
         n = llr.shape[0]
@@ -142,14 +162,15 @@ class OracleCode:
             raise RuntimeError(f"orc_gen_llr rc={rc}")
         return llr, cw
 
-    def wms_loss_grad(self, llr, cw_packed, n_iter, w, want_grad=True):
+    def wms_loss_grad(self, llr, cw_packed, n_iter, w, want_grad=True, layered=False):
         llr = np.ascontiguousarray(llr, np.float32).reshape(-1, self.n_bp)
         n = llr.shape[0]
         w = np.ascontiguousarray(w, np.float64).reshape(n_iter, self.n_edges)
         grad = np.zeros_like(w) if want_grad else None
         app = np.zeros((n, self.n_bp), np.float64)
-        loss = lib().orc_wms_loss_grad_f64(self._h, llr, np.ascontiguousarray(cw_packed, np.uint8),
-                                           n, int(n_iter), w, _ptr(grad), _ptr(app))
+        fn = lib().orc_wms_layered_loss_grad_f64 if layered else lib().orc_wms_loss_grad_f64
+        loss = fn(self._h, llr, np.ascontiguousarray(cw_packed, np.uint8), n, int(n_iter), w, _ptr(grad),
+                  _ptr(app))
         return loss, grad, app
 
     def wms_decode_f32(self, llr, n_iter, w, early_stop=False, want_app=False):

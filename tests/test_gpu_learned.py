@@ -101,3 +101,41 @@ def test_short_training_lowers_the_loss(gpu):
     hist = tr.train(25)
     assert np.mean(hist[-5:]) < np.mean(hist[:5])
     assert np.isfinite(hist).all()
+
+
+@pytest.mark.parametrize("bg,z", [(2, 16), (1, 12), (2, 64)])
+def test_layered_forward_and_adjoint_match_oracle(gpu, bg, z):
+    T, n = 4, 6
+    oc, llr, cw = _data(bg, z, n, 11 + z)
+    rng = np.random.default_rng(z + 1)
+    llr[:, :2 * z] = rng.normal(0, 0.3, (n, 2 * z)).astype(np.float32)
+    w = rng.uniform(0.55, 0.95, (T, oc.n_edges)).astype(np.float32)
+    tr = Trainer(bg=bg, z=z, n_iter=T, batch=n, chunk=n, schedule="layered")
+    wd = torch.from_numpy(w).to(gpu)
+    loss, grad = tr.loss_and_grad(torch.from_numpy(llr).to(gpu), torch.from_numpy(cw).to(gpu), wd)
+    oloss, ograd, _ = oc.wms_loss_grad(llr, cw, T, w.astype(np.float64), layered=True)
+    assert abs(loss - oloss) <= 1e-5 * abs(oloss)
+    g = grad.cpu().numpy()
+    rel = np.linalg.norm(g - ograd) / np.linalg.norm(ograd)
+    assert rel < 2e-3, rel
+    assert np.corrcoef(g.ravel(), ograd.ravel())[0, 1] > 0.9999
+
+
+def test_layered_forward_posterior_is_the_layered_decoder(gpu):
+    bg, z, T, n = 1, 64, 5, 5
+    oc, llr, cw = _data(bg, z, n, 19)
+    w = np.random.default_rng(4).uniform(0.6, 0.9, (T, oc.n_edges)).astype(np.float32)
+    tr = Trainer(bg=bg, z=z, n_iter=T, batch=n, chunk=n, schedule="layered")
+    app = torch.empty((n, oc.n_bp), device=gpu)
+    tr.forward(torch.from_numpy(llr).to(gpu), torch.from_numpy(cw).to(gpu), 1.0, app=app,
+               weights=torch.from_numpy(w).to(gpu))
+    torch.cuda.synchronize()
+    opk, oapp, _ = oc.layered_f32(llr, T, w=w, want_app=True)
+    np.testing.assert_array_equal(app.cpu().numpy().view(np.uint32), oapp.view(np.uint32))
+
+
+def test_layered_short_training_lowers_the_loss(gpu):
+    tr = Trainer(bg=2, z=32, n_iter=4, batch=2048, chunk=1024, lr=5e-3, seed=3, schedule="layered")
+    hist = tr.train(25)
+    assert np.mean(hist[-5:]) < np.mean(hist[:5])
+    assert np.isfinite(hist).all()

@@ -60,3 +60,39 @@ def test_loss_posterior_equals_f64_decoder_at_constant_weight():
     _, _, app = oc.wms_loss_grad(llr, cw, 3, w, want_grad=False)
     _, a64, _ = oc.minsum_f64(llr.astype(np.float64), 3)
     np.testing.assert_allclose(app, a64, rtol=1e-12, atol=1e-12)
+
+
+def test_layered_adjoint_matches_finite_differences():
+    """The layered weighted min-sum adjoint (rows reversed, per-edge dloss/dR
+    carried between iterations) against central differences."""
+    oc, llr, cw, w = _case(bg=2, z=6, n=3, T=3, seed=4)
+    T = w.shape[0]
+    loss, grad, _ = oc.wms_loss_grad(llr, cw, T, w, layered=True)
+    rng = np.random.default_rng(2)
+    checked = 0
+    for _ in range(30):
+        t, e = int(rng.integers(T)), int(rng.integers(oc.n_edges))
+        fd = []
+        for eps in (1e-5, 5e-6):
+            wp, wm = w.copy(), w.copy()
+            wp[t, e] += eps
+            wm[t, e] -= eps
+            lp, _, _ = oc.wms_loss_grad(llr, cw, T, wp, want_grad=False, layered=True)
+            lm, _, _ = oc.wms_loss_grad(llr, cw, T, wm, want_grad=False, layered=True)
+            fd.append((lp - lm) / (2 * eps))
+        if abs(fd[0] - fd[1]) > 1e-6 * max(1.0, abs(fd[0])) * 1e3:
+            continue
+        np.testing.assert_allclose(grad[t, e], fd[0], rtol=2e-4, atol=1e-9)
+        checked += 1
+    assert checked >= 24
+    assert np.abs(grad).max() > 0
+
+
+def test_layered_loss_posterior_equals_layered_f32_decoder():
+    """The f64 layered forward at constant weight 0.75 agrees with the fp32
+    layered decoder to fp32 accuracy."""
+    oc, llr, cw, _ = _case(bg=1, z=8, n=2, T=3, seed=6)
+    w = np.full((3, oc.n_edges), 0.75)
+    _, _, app = oc.wms_loss_grad(llr, cw, 3, w, want_grad=False, layered=True)
+    _, a32, _ = oc.layered_f32(llr, 3, want_app=True)
+    np.testing.assert_allclose(app, a32, rtol=1e-4, atol=1e-4)
