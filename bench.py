@@ -9,6 +9,11 @@ the same metric through the reference-shaped host call
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
+``learned_vs_plain`` (in the same line) compares the learned decoder with plain
+min-sum at a stated Eb/N0 where plain flooding at 10 iterations has FER <=
+1e-2: FER with 95% intervals over 65,536 fresh codewords and info Gbit/s of
+each (early stop on for both).
+
 Under torchrun each rank decodes its own batch (codewords are independent:
 replicas, weak scaling); rank 0 prints one JSON line with the max time over
 ranks.  ``--impl reference`` times the reference algorithm's CPU
@@ -156,53 +161,74 @@ def run_e2e(dec, llr, packed, steps, stream, world):
     return e2e_ms
 
 
-def learned_vs_plain(dec, stream, batch: int, ebn0: float = 1.75, weights: str = "bg1_T10",
-                     frames: int = 32768, timed_steps: int = 10):
-    """Both decoders at one Eb/N0, early stop on: the smallest iteration cap
-    whose FER over `frames` fresh codewords is <= 1e-2, then info Gbit/s of
-    that configuration (LLRs resident, CUDA events).  Iterations past the
-    trained ones reuse the last weight row."""
+def learned_vs_plain(dec, stream, batch: int, ebn0: float = 1.8, frames: int = 65536,
+                     timed_steps: int = 10):
+    """The learned decoder against plain min-sum at one stated Eb/N0 (1.8 dB,
+    where plain flooding min-sum at 10 iterations has FER <= 1e-2), early stop
+    on for both, `frames` fresh codewords per configuration:
+      plain   - the reference's decoder: flooding, alpha 0.75, 10 iterations;
+      learned - layered weighted min-sum with the GPU-trained weights
+                weights/bg1_L6, at the smallest cap in 4..6 iterations whose
+                FER is at most plain's.
+    Info Gbit/s of each is timed with CUDA events on resident LLRs.  Two more
+    points show where the gain comes from: the layered schedule without
+    weights (alpha 0.75) at the learned cap, and the flooding decoder with
+    its own trained weights (weights/bg1_T10) at 10 iterations."""
     import torch
     from nr_ldpc_gb300 import codes
+    from nr_ldpc_gb300.evaluate import clopper_pearson
     from nr_ldpc_gb300.learned import load_weights
     sigma = codes.noise_sigma(ebn0, K_INFO / (N_BP - 2 * Z))
     sig = torch.full((batch,), sigma, dtype=torch.float32, device="cuda")
-    sets = [dec.gen_llr(seed=31, cw_base=(1 << 40) + k * batch, sigma=sig) for k in range(frames // batch)]
-    dec.set_weights(load_weights(weights))
     out = torch.empty((batch, dec.packed_bytes), dtype=torch.uint8, device="cuda")
-    res = {}
-    for name, weighted, caps in (("plain", False, (10, 11, 12, 13, 14, 16, 18, 20)),
-                                 ("learned", True, (8, 9, 10, 11, 12, 14, 16, 18, 20))):
-        for cap in caps:
-            counts = torch.zeros(2, dtype=torch.int64, device="cuda")
-            its = torch.zeros(1, dtype=torch.int64, device="cuda")
-            for llr, cw in sets:
-                pk, it = dec.decode(llr, cap, early_stop=True, weighted=weighted, want_iters=True, out=out)
-                dec.count_errors(pk, cw, counts=counts)
-                its += it.sum()
-            torch.cuda.synchronize()
-            fer = int(counts[1]) / (len(sets) * batch)
-            if fer <= 1e-2 or cap == caps[-1]:
-                break
-        llr, _ = sets[0]
+    n_sets = max(1, frames // batch)
+    launches = 0
+
+    def run(sched, weights, cap):
+        nonlocal launches
+        dec.set_schedule(sched)
+        if weights is not None:
+            dec.set_weights(load_weights(weights))
+        weighted = weights is not None
+        counts = torch.zeros(2, dtype=torch.int64, device="cuda")
+        its = torch.zeros(1, dtype=torch.int64, device="cuda")
+        for k in range(n_sets):
+            llr, cw = dec.gen_llr(seed=31, cw_base=(1 << 40) + k * batch, sigma=sig)
+            pk, it = dec.decode(llr, cap, early_stop=True, weighted=weighted, want_iters=True, out=out)
+            dec.count_errors(pk, cw, counts=counts)
+            its += it.sum()
+        llr, _ = dec.gen_llr(seed=31, cw_base=(1 << 40), sigma=sig)
         for _ in range(3):
-            dec.decode(llr, cap, early_stop=True, weighted=weighted, out=out)
+            dec.decode(llr, cap, early_stop=True, weighted=weighted, out=out, stream=stream)
+        torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(timed_steps):
             dec.decode(llr, cap, early_stop=True, weighted=weighted, out=out, stream=stream)
         e1.record(stream)
         torch.cuda.synchronize()
+        launches += 3 * n_sets + 4 + timed_steps
         ms = e0.elapsed_time(e1) / timed_steps
-        res[name] = {"iters_max": cap, "fer": fer, "frames": len(sets) * batch,
-                     "avg_iters": float(its.item()) / (len(sets) * batch),
-                     "info_gbps": batch * K_INFO / (ms * 1e-3) / 1e9, "ms_per_batch": ms}
-    res["learned"]["weights"] = weights
-    res["plain"]["alpha"] = 0.75
-    res["ebn0_db"] = ebn0
-    res["early_stop"] = True
-    res["speedup"] = res["learned"]["info_gbps"] / res["plain"]["info_gbps"]
-    return res, 1 + 2 * timed_steps + 6
+        n = n_sets * batch
+        fe = int(counts[1])
+        lo, hi = clopper_pearson(fe, n)
+        return {"schedule": sched, "weights": weights or "alpha 0.75", "iters_max": cap, "fer": fe / n,
+                "fer_ci95": [lo, hi], "frames": n, "avg_iters": float(its.item()) / n,
+                "info_gbps": batch * K_INFO / (ms * 1e-3) / 1e9, "ms_per_batch": ms}
+
+    plain = run("flooding", None, ITERS)
+    learned = None
+    for cap in (4, 5, 6):
+        learned = run("layered", "bg1_L6", cap)
+        if learned["fer"] <= plain["fer"]:
+            break
+    res = {"ebn0_db": ebn0, "early_stop": True, "plain": plain, "learned": learned,
+           "learned_matches_plain_fer": learned["fer"] <= plain["fer"],
+           "speedup": learned["info_gbps"] / plain["info_gbps"],
+           "layered_without_weights": run("layered", None, learned["iters_max"]),
+           "flooding_learned_T10": run("flooding", "bg1_T10", ITERS)}
+    dec.set_schedule("flooding")
+    return res, launches
 
 
 def cpu_baseline(llr_host: np.ndarray, n_sample: int):

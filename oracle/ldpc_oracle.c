@@ -798,6 +798,9 @@ double orc_wms_loss_grad_f64(const orc_code* c, const float* llr, const uint8_t*
     return loss;
 }
 
+double orc_wms_layered_loss_grad(const orc_code* c, const float* llr, const uint8_t* cw_packed, int n_cw,
+                                 int n_iter, const double* w, double* grad, double* app, int f32_forward);
+
 /* Layered weighted min-sum: forward + adjoint in double precision.  No
  * reference counterpart.  Forward per iteration t, rows ascending:
  *   Q^t_e = A[col] - R^{t-1}_e;  R^t_e = w[t][e] * sign_e * min_e;
@@ -808,6 +811,14 @@ double orc_wms_loss_grad_f64(const orc_code* c, const float* llr, const uint8_t*
  *   h_e <- -dQ_e for iteration t-1. */
 double orc_wms_layered_loss_grad_f64(const orc_code* c, const float* llr, const uint8_t* cw_packed,
                                      int n_cw, int n_iter, const double* w, double* grad, double* app) {
+    return orc_wms_layered_loss_grad(c, llr, cw_packed, n_cw, n_iter, w, grad, app, 0);
+}
+
+/* f32_forward != 0: the forward runs in fp32 with the decoder's rounding
+ * (Q = fl(A - R_old), R = +-fl(w * min), A = fl(Q + R)), so its argmins and
+ * signs are the GPU forward's exactly; the loss and adjoint stay in double. */
+double orc_wms_layered_loss_grad(const orc_code* c, const float* llr, const uint8_t* cw_packed, int n_cw,
+                                 int n_iter, const double* w, double* grad, double* app, int f32_forward) {
     const int z = c->z, N = c->cols * z, E = c->n_edges, EZ = E * z, T = n_iter;
     double* Qs = (double*)malloc(sizeof(double) * (size_t)T * EZ); /* Q^t per edge */
     double* Ah = (double*)malloc(sizeof(double) * (size_t)T * N);  /* A after iteration t */
@@ -832,7 +843,8 @@ double orc_wms_layered_loss_grad_f64(const orc_code* c, const float* llr, const 
                     double m1 = 1000.0, m2 = 1000.0;
                     for (int i = 0; i < deg; i++) {
                         const int e = e0 + i;
-                        const double q = A[edge_col(c, e, s)] - R[e * z + s];
+                        const double q = f32_forward ? (double)((float)A[edge_col(c, e, s)] - (float)R[e * z + s])
+                                                     : A[edge_col(c, e, s)] - R[e * z + s];
                         Qt[e * z + s] = q;
                         const double qa = fabs(q);
                         q_sign ^= (q < 0) << i;
@@ -843,8 +855,14 @@ double orc_wms_layered_loss_grad_f64(const orc_code* c, const float* llr, const 
                         const int e = e0 + i;
                         const int sb = par ^ ((q_sign >> i) & 1);
                         const double mag = i != i1 ? m1 : m2;
-                        R[e * z + s] = w[t * E + e] * (sb ? -mag : mag);
-                        A[edge_col(c, e, s)] = Qt[e * z + s] + R[e * z + s];
+                        if (f32_forward) {
+                            const float rm = (float)w[t * E + e] * (float)mag;
+                            R[e * z + s] = sb ? -rm : rm;
+                            A[edge_col(c, e, s)] = (double)((float)Qt[e * z + s] + (float)R[e * z + s]);
+                        } else {
+                            R[e * z + s] = w[t * E + e] * (sb ? -mag : mag);
+                            A[edge_col(c, e, s)] = Qt[e * z + s] + R[e * z + s];
+                        }
                     }
                 }
             }

@@ -132,6 +132,10 @@ int orc_layered_f32(const orc_code* c, const float* llr, int n_cw, int n_iter, f
  * loss as orc_wms_loss_grad_f64, posterior updated row by row in place). */
 double orc_wms_layered_loss_grad_f64(const orc_code* c, const float* llr, const uint8_t* cw_packed,
                                      int n_cw, int n_iter, const double* w, double* grad, double* app);
+/* As above; f32_forward != 0 runs the forward in fp32 with the decoder's
+ * rounding (the GPU forward's argmins and signs), loss and adjoint in double. */
+double orc_wms_layered_loss_grad(const orc_code* c, const float* llr, const uint8_t* cw_packed, int n_cw,
+                                 int n_iter, const double* w, double* grad, double* app, int f32_forward);
 
 #ifdef __cplusplus
 }

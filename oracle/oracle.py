@@ -62,6 +62,9 @@ def lib():
         L.orc_wms_layered_loss_grad_f64.restype = C.c_double
         L.orc_wms_layered_loss_grad_f64.argtypes = [C.c_void_p, _f32p, _u8p, C.c_int, C.c_int, _f64p,
                                                     C.c_void_p, C.c_void_p]
+        L.orc_wms_layered_loss_grad.restype = C.c_double
+        L.orc_wms_layered_loss_grad.argtypes = [C.c_void_p, _f32p, _u8p, C.c_int, C.c_int, _f64p,
+                                                C.c_void_p, C.c_void_p, C.c_int]
         L.orc_wms_decode_f32.argtypes = [C.c_void_p, _f32p, C.c_int, C.c_int, _f32p, C.c_int,
                                          C.c_int, _u8p, C.c_void_p, C.c_void_p]
         L.orc_layered_f32.argtypes = [C.c_void_p, _f32p, C.c_int, C.c_int, C.c_float, C.c_void_p,
@@ -162,15 +165,21 @@ class OracleCode:
             raise RuntimeError(f"orc_gen_llr rc={rc}")
         return llr, cw
 
-    def wms_loss_grad(self, llr, cw_packed, n_iter, w, want_grad=True, layered=False):
+    def wms_loss_grad(self, llr, cw_packed, n_iter, w, want_grad=True, layered=False, f32_forward=False):
+        """Loss, dloss/dw and final posterior of the weighted decoder (f64;
+        layered: the row-sequential schedule, f32_forward: its forward in the
+        decoder's fp32 rounding)."""
         llr = np.ascontiguousarray(llr, np.float32).reshape(-1, self.n_bp)
         n = llr.shape[0]
         w = np.ascontiguousarray(w, np.float64).reshape(n_iter, self.n_edges)
         grad = np.zeros_like(w) if want_grad else None
         app = np.zeros((n, self.n_bp), np.float64)
-        fn = lib().orc_wms_layered_loss_grad_f64 if layered else lib().orc_wms_loss_grad_f64
-        loss = fn(self._h, llr, np.ascontiguousarray(cw_packed, np.uint8), n, int(n_iter), w, _ptr(grad),
-                  _ptr(app))
+        cw = np.ascontiguousarray(cw_packed, np.uint8)
+        if layered:
+            loss = lib().orc_wms_layered_loss_grad(self._h, llr, cw, n, int(n_iter), w, _ptr(grad), _ptr(app),
+                                                   int(f32_forward))
+        else:
+            loss = lib().orc_wms_loss_grad_f64(self._h, llr, cw, n, int(n_iter), w, _ptr(grad), _ptr(app))
         return loss, grad, app
 
     def wms_decode_f32(self, llr, n_iter, w, early_stop=False, want_app=False):

@@ -113,11 +113,14 @@ def test_layered_forward_and_adjoint_match_oracle(gpu, bg, z):
     tr = Trainer(bg=bg, z=z, n_iter=T, batch=n, chunk=n, schedule="layered")
     wd = torch.from_numpy(w).to(gpu)
     loss, grad = tr.loss_and_grad(torch.from_numpy(llr).to(gpu), torch.from_numpy(cw).to(gpu), wd)
-    oloss, ograd, _ = oc.wms_loss_grad(llr, cw, T, w.astype(np.float64), layered=True)
+    # the oracle's forward in the decoder's fp32 rounding: same argmins and
+    # signs as the GPU (an f64 forward flips near-tied argmins of the
+    # sequential in-place updates); loss and adjoint in double
+    oloss, ograd, _ = oc.wms_loss_grad(llr, cw, T, w.astype(np.float64), layered=True, f32_forward=True)
     assert abs(loss - oloss) <= 1e-5 * abs(oloss)
     g = grad.cpu().numpy()
     rel = np.linalg.norm(g - ograd) / np.linalg.norm(ograd)
-    assert rel < 2e-3, rel
+    assert rel < 2e-4, rel
     assert np.corrcoef(g.ravel(), ograd.ravel())[0, 1] > 0.9999
 
 

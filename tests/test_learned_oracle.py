@@ -96,3 +96,14 @@ def test_layered_loss_posterior_equals_layered_f32_decoder():
     _, _, app = oc.wms_loss_grad(llr, cw, 3, w, want_grad=False, layered=True)
     _, a32, _ = oc.layered_f32(llr, 3, want_app=True)
     np.testing.assert_allclose(app, a32, rtol=1e-4, atol=1e-4)
+
+
+def test_layered_f32_forward_matches_layered_decoder():
+    """The fp32-forward variant of the layered loss reproduces the fp32
+    layered decoder's posterior bit for bit (it is the GPU forward)."""
+    oc, llr, cw, w = _case(bg=1, z=8, n=2, T=3, seed=8)
+    w32 = w.astype(np.float32)
+    _, _, app = oc.wms_loss_grad(llr, cw, 3, w32.astype(np.float64), want_grad=False, layered=True,
+                                 f32_forward=True)
+    _, a32, _ = oc.layered_f32(llr, 3, w=w32, want_app=True)
+    np.testing.assert_array_equal(app.astype(np.float32).view(np.uint32), a32.view(np.uint32))
