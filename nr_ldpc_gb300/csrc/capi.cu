@@ -19,6 +19,7 @@ namespace {
 #include "base_graphs.inc"
 
 const int kBaseZ[8] = {2, 3, 5, 7, 9, 11, 13, 15};
+constexpr int kHostChunks = 16;  // most chunks of one host-buffer decode
 
 struct Handle {
     int device = 0;
@@ -38,6 +39,10 @@ struct Handle {
     int n_w_iters = 0;
     bool wms_ready = false;
     int schedule = NRLDPC_SCHEDULE_FLOODING;
+    // host-buffer pipeline: copies of chunk k+1 overlap the decode of chunk k
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_start = nullptr;
+    cudaEvent_t ev_chunk[kHostChunks] = {};
 };
 
 int map_cuda(cudaError_t e) { return e == cudaSuccess ? NRLDPC_OK : NRLDPC_ERR_CUDA; }
@@ -132,6 +137,10 @@ void free_handle(Handle* h) {
     cudaFree(h->stage_packed);
     cudaFree(h->stage_q);
     cudaFree(h->weights);
+    for (cudaEvent_t e : h->ev_chunk)
+        if (e) cudaEventDestroy(e);
+    if (h->ev_start) cudaEventDestroy(h->ev_start);
+    if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     delete h;
 }
 
@@ -193,11 +202,18 @@ int init_impl(const int* base, int rows, int cols, int kb, const nrldpc_config* 
     if (cudaMalloc(&h->state, state_elems * kStateBytesPerRow) != cudaSuccess ||
         cudaMalloc(&h->scratch, 64) != cudaSuccess || cudaMemset(h->scratch, 0, 64) != cudaSuccess ||
         cudaMalloc(&h->stage_llr, n_llr * sizeof(float)) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_start, cudaEventDisableTiming) != cudaSuccess ||
         cudaMalloc(&h->stage_packed,
                    static_cast<size_t>(cfg->max_batch) * h->tab.packed_bytes) != cudaSuccess) {
         free_handle(h);
         return NRLDPC_ERR_NO_MEMORY;
     }
+    for (cudaEvent_t& e : h->ev_chunk)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+            free_handle(h);
+            return NRLDPC_ERR_CUDA;
+        }
     *out = reinterpret_cast<nrldpc_handle*>(h);
     return NRLDPC_OK;
 }
@@ -231,6 +247,48 @@ int decode_impl(Handle* h, const float* llr, uint8_t* packed, int n_cw, int n_it
     if (e != cudaSuccess) return NRLDPC_ERR_CUDA;
     return map_cuda(launch_decode(h->tab, a, grid, h->threads, h->smem, weighted,
                                   h->schedule == NRLDPC_SCHEDULE_LAYERED, h->minb, stream));
+}
+
+// Host-buffer decode (fp32 LLRs, or narrow ones widened on the GPU: qtype 1
+// fp16, 2 int8 * scale).  The batch is cut into chunks of whole CTA rounds
+// (1, 2, then 4 rounds of max_grid * cpb codewords): chunk k+1's host->device
+// copy runs on the handle's copy stream while chunk k decodes on the caller's
+// stream, and each chunk's packed bits go back as soon as it is decoded.
+int host_decode(Handle* h, const void* h_llr, int qtype, float scale, uint8_t* h_packed, int n_cw, int n_iter,
+                int early, cudaStream_t s) {
+    const size_t n_bp = static_cast<size_t>(h->tab.n_bp);
+    const size_t in_elem = qtype == 0 ? 4 : (qtype == 1 ? 2 : 1);
+    const size_t round = static_cast<size_t>(h->max_grid) * h->cpb;
+    void* stage_in = qtype == 0 ? static_cast<void*>(h->stage_llr) : h->stage_q;
+    // the copy stream must not overwrite staging a previous call still reads
+    if (cudaEventRecord(h->ev_start, s) != cudaSuccess ||
+        cudaStreamWaitEvent(h->copy_stream, h->ev_start, 0) != cudaSuccess)
+        return NRLDPC_ERR_CUDA;
+    size_t begin = 0;
+    size_t rounds = 1;
+    for (int k = 0; begin < static_cast<size_t>(n_cw); k++) {
+        size_t count = std::min(static_cast<size_t>(n_cw) - begin, rounds * round);
+        if (k == kHostChunks - 1) count = static_cast<size_t>(n_cw) - begin;  // last event: the rest
+        rounds = std::min<size_t>(rounds * 2, 4);
+        const char* src = static_cast<const char*>(h_llr) + begin * n_bp * in_elem;
+        char* dst = static_cast<char*>(stage_in) + begin * n_bp * in_elem;
+        if (cudaMemcpyAsync(dst, src, count * n_bp * in_elem, cudaMemcpyHostToDevice, h->copy_stream) !=
+                cudaSuccess ||
+            cudaEventRecord(h->ev_chunk[k], h->copy_stream) != cudaSuccess ||
+            cudaStreamWaitEvent(s, h->ev_chunk[k], 0) != cudaSuccess)
+            return NRLDPC_ERR_CUDA;
+        float* llr = h->stage_llr + begin * n_bp;
+        if (qtype != 0 && launch_dequant(dst, qtype, scale, count * n_bp, llr, s) != cudaSuccess)
+            return NRLDPC_ERR_CUDA;
+        uint8_t* out = h->stage_packed + begin * h->tab.packed_bytes;
+        const int rc = decode_impl(h, llr, out, static_cast<int>(count), n_iter, early, nullptr, nullptr, false, s);
+        if (rc) return rc;
+        if (cudaMemcpyAsync(h_packed + begin * h->tab.packed_bytes, out, count * h->tab.packed_bytes,
+                            cudaMemcpyDeviceToHost, s) != cudaSuccess)
+            return NRLDPC_ERR_CUDA;
+        begin += count;
+    }
+    return NRLDPC_OK;
 }
 
 }  // namespace
@@ -385,15 +443,9 @@ int nrldpc_decode_host_async(nrldpc_handle* handle, const float* h_llr, uint8_t*
     if (!h || !h_llr || !h_packed || n_cw < 0) return NRLDPC_ERR_INVALID_ARG;
     if (n_cw > h->max_batch) return NRLDPC_ERR_TOO_LARGE;
     if (n_cw == 0) return NRLDPC_OK;
-    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    const size_t in_bytes = static_cast<size_t>(n_cw) * h->tab.n_bp * sizeof(float);
-    const size_t out_bytes = static_cast<size_t>(n_cw) * h->tab.packed_bytes;
-    if (cudaMemcpyAsync(h->stage_llr, h_llr, in_bytes, cudaMemcpyHostToDevice, s) != cudaSuccess)
-        return NRLDPC_ERR_CUDA;
-    const int rc = decode_impl(h, h->stage_llr, h->stage_packed, n_cw, n_iter, early_stop, nullptr,
-                               nullptr, false, s);
-    if (rc) return rc;
-    return map_cuda(cudaMemcpyAsync(h_packed, h->stage_packed, out_bytes, cudaMemcpyDeviceToHost, s));
+    if (n_iter < 1 || (early_stop != 0 && early_stop != 1)) return NRLDPC_ERR_INVALID_ARG;
+    return host_decode(h, h_llr, 0, 1.0f, h_packed, n_cw, n_iter, early_stop,
+                       reinterpret_cast<cudaStream_t>(stream));
 }
 
 int nrldpc_decode_host_async_q(nrldpc_handle* handle, const void* h_llr_q, int qtype, float scale,
@@ -405,9 +457,7 @@ int nrldpc_decode_host_async_q(nrldpc_handle* handle, const void* h_llr_q, int q
     if (n_cw > h->max_batch) return NRLDPC_ERR_TOO_LARGE;
     if (n_cw == 0) return NRLDPC_OK;
     if (!h_llr_q || !h_packed) return NRLDPC_ERR_INVALID_ARG;
-    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
-    const size_t n = static_cast<size_t>(n_cw) * h->tab.n_bp;
-    const size_t qbytes = n * (qtype == 1 ? 2 : 1);
+    if (n_iter < 1 || (early_stop != 0 && early_stop != 1)) return NRLDPC_ERR_INVALID_ARG;
     if (!h->stage_q) {  // narrow staging, allocated on the first call of this entry point
         const size_t cap = static_cast<size_t>(h->max_batch) * h->tab.n_bp * 2;
         if (cudaMalloc(&h->stage_q, cap) != cudaSuccess) {
@@ -415,16 +465,8 @@ int nrldpc_decode_host_async_q(nrldpc_handle* handle, const void* h_llr_q, int q
             return NRLDPC_ERR_NO_MEMORY;
         }
     }
-    void* narrow = h->stage_q;
-    if (cudaMemcpyAsync(narrow, h_llr_q, qbytes, cudaMemcpyHostToDevice, s) != cudaSuccess)
-        return NRLDPC_ERR_CUDA;
-    if (launch_dequant(narrow, qtype, scale, n, h->stage_llr, s) != cudaSuccess) return NRLDPC_ERR_CUDA;
-    const int rc = decode_impl(h, h->stage_llr, h->stage_packed, n_cw, n_iter, early_stop, nullptr,
-                               nullptr, false, s);
-    if (rc) return rc;
-    return map_cuda(cudaMemcpyAsync(h_packed, h->stage_packed,
-                                    static_cast<size_t>(n_cw) * h->tab.packed_bytes,
-                                    cudaMemcpyDeviceToHost, s));
+    return host_decode(h, h_llr_q, qtype, scale, h_packed, n_cw, n_iter, early_stop,
+                       reinterpret_cast<cudaStream_t>(stream));
 }
 
 int nrldpc_set_schedule(nrldpc_handle* handle, int schedule) {

@@ -8,7 +8,7 @@
 //     row (min1, min2, argmin + R sign bits, and the posterior of the row's
 //     degree-1 suffix column) as one uint4 per (row, sub-row), in a per-CTA
 //     slot of global memory that stays L2-resident (each CTA reuses its slot
-//     for every codeword it takes), requested three rows ahead.  Keeping the
+//     for every codeword it takes), requested two rows ahead.  Keeping the
 //     suffix columns (5G NR: the extension parity, 42 of 68 BG1 columns) out
 //     of shared memory halves it, so two CTAs run per SM.
 // The core LLRs come into shared memory with one cp.async.bulk copy per
@@ -309,8 +309,8 @@ __device__ __forceinline__ void write_outputs(const CodeTable& tab, const float*
 }
 
 // All base rows of one iteration, ascending; returns the OR of the row
-// parities of the hard decisions read (CHECK only).  The state of row r+3 is
-// requested while row r runs (L2 latency spans several rows); in the first
+// parities of the hard decisions read (CHECK only).  The state of row r+2 is
+// requested while row r runs (L2 latency spans more than one row); in the first
 // iteration the state is zero and only the suffix posterior is fetched, from
 // the codeword's LLRs in global memory.
 //   store: write this iteration's state; write_hd: write the suffix hard
@@ -332,9 +332,9 @@ __device__ __forceinline__ uint32_t iterate_rows(const CodeTable& tab, uint32_t 
         if (tab.row_sfx[r]) v.w = __float_as_uint(__ldcs(gllr + edge_pos(tab, tab.row_ptr[r + 1] - 1, s)));
         return v;
     };
-    uint4 s0 = fetch(0), s1 = fetch(1), s2 = fetch(2);
+    uint4 s0 = fetch(0), s1 = fetch(1);
     for (int r = 0; r < rows; r++) {
-        const uint4 s3 = fetch(r + 3);
+        const uint4 s2 = fetch(r + 2);
         if (act) {
             const bool sfx = tab.row_sfx[r] != 0;
             const int e0 = tab.row_ptr[r];
@@ -348,7 +348,6 @@ __device__ __forceinline__ uint32_t iterate_rows(const CodeTable& tab, uint32_t 
         }
         s0 = s1;
         s1 = s2;
-        s2 = s3;
         if (tab.sync_after[r]) __syncthreads();
     }
     return fail;

@@ -223,3 +223,28 @@ def test_reduced_precision_host_transfer(gpu, qtype):
     s.synchronize()
     want, _, _ = oc.minsum_f32(wide, 8)
     np.testing.assert_array_equal(out.numpy(), want)
+
+
+def test_host_call_in_chunks_back_to_back(gpu):
+    """A batch of several CTA rounds goes through the chunked host pipeline
+    (copies of chunk k+1 overlap the decode of chunk k); two calls queued
+    back to back on one stream with different inputs both come out right."""
+    n = 1500  # 304-codeword rounds at BG1 Z=384: chunks of 304, 608, 588
+    dec = Decoder(bg=1, z=384, max_batch=n)
+    sig = torch.full((n,), codes.noise_sigma(1.6, 1 / 3), device=gpu)
+    llr_a, _ = dec.gen_llr(41, 0, sig)
+    llr_b, _ = dec.gen_llr(42, 0, sig)
+    ref_a, ref_b = dec.decode(llr_a, 7).cpu(), dec.decode(llr_b, 7).cpu()
+    h_a, h_b = llr_a.cpu().pin_memory(), llr_b.cpu().pin_memory()
+    out_a = torch.empty((n, dec.packed_bytes), dtype=torch.uint8).pin_memory()
+    out_b = torch.empty_like(out_a).pin_memory()
+    s = torch.cuda.Stream()
+    dec.decode_host(h_a, out_a, 7, stream=s)
+    dec.decode_host(h_b, out_b, 7, stream=s)
+    s.synchronize()
+    assert torch.equal(out_a, ref_a) and torch.equal(out_b, ref_b)
+    q = llr_a.cpu().to(torch.float16)
+    out_q = torch.empty_like(out_a).pin_memory()
+    dec.decode_host_q(q.pin_memory(), out_q, 7, stream=s)
+    s.synchronize()
+    assert torch.equal(out_q, dec.decode(q.to(gpu).float(), 7).cpu())
