@@ -115,24 +115,22 @@ __device__ __forceinline__ uint32_t lds_u8(uint32_t a) {
 // One lifted row (base row with D edges, sub-row s) of one iteration.
 // The first iteration passes a zero state (and a zero previous weight), so
 // R_old = +0 and Q = L - (+0) = L, dt = R - (+0) = R exactly, as in
-// cnp_kernel_1st_iter.  CHECK also accumulates the parity of the hard
-// decisions read (syndrome of the previous iteration).
+// cnp_kernel_1st_iter.
 //   s4old: shared byte address of this slot's Lold plus 4*s;
 //   dnew:  byte distance from Lold to Lnew; z4 = 4*Z;
 //   sfx:   the last edge is a suffix column: its posterior is st.w (read)
 //          and goes to the stored state's w (written), not shared memory;
 //   st:    this row's state from the previous iteration; st_out: where this
 //          iteration's goes, or null;
-//   hd:    shared byte address for the suffix column's hard decisions
-//          (bit 0: posterior read, bit 1: posterior written), or 0;
-//   app_sfx: global slot for the suffix posterior read, or null.
+//   hd:    shared byte address for the suffix column's hard decision of
+//          the posterior written (bit 1), or 0.
 // LAYERED (no reference counterpart): one posterior buffer updated in place,
 // A = Q + R_new (dnew = 0), instead of Lnew += R_new - R_old.
-template <int D, bool WEIGHTED, bool CHECK, bool LAYERED>
+template <int D, bool WEIGHTED, bool LAYERED>
 __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sfx, uint32_t s,
                                            uint32_t s4old, uint32_t dnew, uint32_t z4,
                                            const float2* wpair, uint4 st, uint4* st_out, uint32_t hd,
-                                           float* app_sfx, float alpha, uint32_t& syn) {
+                                           float alpha) {
     constexpr int LAST = D - 1;
     uint32_t addr[D];
     float lv[D];
@@ -172,7 +170,6 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
         const float ro = __uint_as_float(__float_as_uint(mag) | ((oinfo << (23 - i)) & 0x80000000u));
         const float q = __fsub_rn(lv[i], ro);
         keep[i] = LAYERED ? q : ro;
-        if (CHECK) syn ^= (lv[i] > 0.0f) ? 0u : 1u;  // hard decision of the posterior read
         const float qa = fabsf(q);
         if (q < 0.0f) qmask |= 1u << i;
         if (qa < m1) idx = i;
@@ -227,26 +224,23 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
                 sts(addr[i] + dnew, v);
         }
     }
-    if (sfx) {
-        if (hd) sts_u8(hd, (lv[LAST] > 0.0f ? 0u : 1u) | (sfx_new > 0.0f ? 0u : 2u));
-        if (app_sfx) *app_sfx = lv[LAST];
-    }
+    if (sfx && hd) sts_u8(hd, sfx_new > 0.0f ? 0u : 2u);
     if (st_out) {
         const uint32_t info = static_cast<uint32_t>(idx) | ((rsign & ((1u << D) - 1u)) << 8);
         __stcg(st_out, make_uint4(__float_as_uint(m1), __float_as_uint(m2), info, __float_as_uint(sfx_new)));
     }
 }
 
-template <bool WEIGHTED, bool CHECK, bool LAYERED>
+template <bool WEIGHTED, bool LAYERED>
 __device__ __forceinline__ void row_dispatch(int deg, const CodeTable& tab, int e0, bool sfx, uint32_t s,
                                              uint32_t s4old, uint32_t dnew, uint32_t z4,
                                              const float2* wpair, uint4 st, uint4* st_out, uint32_t hd,
-                                             float* app_sfx, float alpha, uint32_t& syn) {
+                                             float alpha) {
     switch (deg) {
 #define NRLDPC_ROW_CASE(D)                                                                         \
     case D:                                                                                        \
-        row_update<D, WEIGHTED, CHECK, LAYERED>(tab, e0, sfx, s, s4old, dnew, z4, wpair, st, st_out, \
-                                                hd, app_sfx, alpha, syn);                          \
+        row_update<D, WEIGHTED, LAYERED>(tab, e0, sfx, s, s4old, dnew, z4, wpair, st, st_out, hd, \
+                                         alpha);                                                  \
         break;
         NRLDPC_ROW_CASE(1) NRLDPC_ROW_CASE(2) NRLDPC_ROW_CASE(3) NRLDPC_ROW_CASE(4)
         NRLDPC_ROW_CASE(5) NRLDPC_ROW_CASE(6) NRLDPC_ROW_CASE(7) NRLDPC_ROW_CASE(8)
@@ -308,23 +302,19 @@ __device__ __forceinline__ void write_outputs(const CodeTable& tab, const float*
     if (iters && s == 0) *iters = it;
 }
 
-// All base rows of one iteration, ascending; returns the OR of the row
-// parities of the hard decisions read (CHECK only).  The state of row r+2 is
-// requested while row r runs (L2 latency spans more than one row); in the first
-// iteration the state is zero and only the suffix posterior is fetched, from
-// the codeword's LLRs in global memory.
+// All base rows of one iteration, ascending.  The state of row r+2 is
+// requested while row r runs (L2 latency spans more than one row); in the
+// first iteration the state is zero and only the suffix posterior is
+// fetched, from the codeword's LLRs in global memory.
 //   store: write this iteration's state; write_hd: write the suffix hard
-//   decisions; app_cw: the codeword's posterior output when the suffix
-//   posteriors read are to be written there.
-template <bool WEIGHTED, bool CHECK, bool LAYERED>
-__device__ __forceinline__ uint32_t iterate_rows(const CodeTable& tab, uint32_t s, uint32_t s4old,
-                                                 uint32_t dnew, const float2* wpair, uint4* st_base,
-                                                 const float* gllr, uint32_t hd_base, float* app_cw,
-                                                 bool act, bool first, bool store, bool write_hd,
-                                                 float alpha) {
+//   decisions.
+template <bool WEIGHTED, bool LAYERED>
+__device__ __forceinline__ void iterate_rows(const CodeTable& tab, uint32_t s, uint32_t s4old, uint32_t dnew,
+                                             const float2* wpair, uint4* st_base, const float* gllr,
+                                             uint32_t hd_base, bool act, bool first, bool store, bool write_hd,
+                                             float alpha) {
     const int z = tab.z, rows = tab.rows;
     const uint32_t z4 = 4u * static_cast<uint32_t>(z);
-    uint32_t fail = 0;
     auto fetch = [&](int r) -> uint4 {
         uint4 v = make_uint4(0u, 0u, 0u, 0u);
         if (!act || r >= rows) return v;
@@ -337,26 +327,23 @@ __device__ __forceinline__ uint32_t iterate_rows(const CodeTable& tab, uint32_t 
         const uint4 s2 = fetch(r + 2);
         if (act) {
             const bool sfx = tab.row_sfx[r] != 0;
-            const int e0 = tab.row_ptr[r];
-            float* app_sfx = (app_cw && sfx) ? app_cw + edge_pos(tab, tab.row_ptr[r + 1] - 1, s) : nullptr;
-            uint32_t syn = 0;
-            row_dispatch<WEIGHTED, CHECK, LAYERED>(tab.row_deg[r], tab, e0, sfx, s, s4old, dnew, z4, wpair, s0,
-                                          store ? st_base + r * z + s : nullptr,
-                                          (write_hd && sfx) ? hd_base + static_cast<uint32_t>(r * z) : 0u,
-                                          app_sfx, alpha, syn);
-            fail |= syn;
+            row_dispatch<WEIGHTED, LAYERED>(tab.row_deg[r], tab, tab.row_ptr[r], sfx, s, s4old, dnew, z4, wpair,
+                                            s0, store ? st_base + r * z + s : nullptr,
+                                            (write_hd && sfx) ? hd_base + static_cast<uint32_t>(r * z) : 0u,
+                                            alpha);
         }
         s0 = s1;
         s1 = s2;
         if (tab.sync_after[r]) __syncthreads();
     }
-    return fail;
 }
 
-// Syndrome of the slot's hard decisions after a layered iteration: sets
-// *fail when a lifted check is unsatisfied.  Core columns are read from the
-// posterior buffer, suffix columns from bit 1 of their hard-decision bytes.
-// Threads stop at the first failure seen by any thread of the slot.
+// Syndrome of the slot's hard decisions after an iteration: sets *fail when
+// a lifted check is unsatisfied.  Core columns are read from the posterior
+// just written (s4a: its shared address plus 4*s), suffix columns from bit 1
+// of their hard-decision bytes.  Threads stop at the first failure seen by
+// any thread of the slot, so an iteration far from convergence costs a few
+// rows.
 __device__ __forceinline__ void check_rows(const CodeTable& tab, uint32_t s, uint32_t s4a, uint32_t hd_base,
                                            volatile int* fail) {
     const int z = tab.z;
@@ -387,8 +374,10 @@ struct SlotOut {
 // All iterations of one codeword group whose core LLRs are already in buf0
 // (Lold): cpb slots, this thread = sub-row s of slot `slot`; gllr = the
 // slot's codeword in global memory (suffix LLRs).  Ends with a barrier.
-// LAYERED: Lold is the one posterior buffer; early stop checks the syndrome
-// after each iteration in a separate pass.
+// Flooding accumulates into Lnew and copies it back to Lold; LAYERED updates
+// Lold in place.  Early stop: after iteration t < n_iter - 1, a codeword
+// whose hard decisions satisfy every check stops with iters = t + 1 (the
+// oracle's rule, ldpc_oracle.c decode_one_f32).
 template <bool WEIGHTED, bool LAYERED>
 __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slot, uint32_t s,
                                           bool slot_done, float* buf0, uint8_t* hd0, float2* wpair,
@@ -397,7 +386,7 @@ __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slo
                                           int n_w_iters) {
     const int z = tab.z, cf = tab.core_floats, tid = threadIdx.x;
     float* lold = buf0 + static_cast<size_t>(slot) * cf;  // read by the check-node pass
-    float* lnew = lold + static_cast<size_t>(cpb) * cf;   // accumulates the new posterior
+    float* lnew = LAYERED ? lold : lold + static_cast<size_t>(cpb) * cf;  // the posterior written
     const uint8_t* hd = hd0 + static_cast<size_t>(slot) * tab.rows * z;
     const uint32_t s4old = smem_addr(lold) + 4u * s;
     const uint32_t dnew = LAYERED ? 0u : static_cast<uint32_t>(cpb) * static_cast<uint32_t>(cf) * 4u;
@@ -417,39 +406,14 @@ __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slo
         __syncthreads();
         const bool act = !slot_done;
         const bool store = !last || out.app != nullptr;
-        if (LAYERED) {
-            const bool check = early_stop && !last;
-            iterate_rows<WEIGHTED, false, true>(tab, s, s4old, 0u, wpair, st_base, gllr, hd_base, nullptr, act,
-                                                first, store, early_stop || last, alpha);
-            if (check) {
-                if (act) check_rows(tab, s, s4old, hd_base, &s_fail[slot]);
-                __syncthreads();
-                const bool conv = act && s_fail[slot] == 0;
-                if (conv)  // HD of this iteration is a codeword
-                    write_outputs(tab, lold, hd, 1, st_base, s, out.packed, out.app, out.iters, t + 1, true);
-                slot_done = slot_done || conv;
-                if (__syncthreads_and(slot_done)) break;
-            }
-            if (last) {
-                if (!slot_done) write_outputs(tab, lold, hd, 1, st_base, s, out.packed, out.app, out.iters, n_iter, true);
-                break;
-            }
-            continue;
-        }
-        const bool check = early_stop && t > 0;
-        const bool write_hd = check || last;
-        float* app_cw = (check && out.app) ? out.app : nullptr;
-        const uint32_t fail =
-            check ? iterate_rows<WEIGHTED, true, false>(tab, s, s4old, dnew, wpair, st_base, gllr, hd_base,
-                                                       app_cw, act, first, store, write_hd, alpha)
-                  : iterate_rows<WEIGHTED, false, false>(tab, s, s4old, dnew, wpair, st_base, gllr, hd_base,
-                                                        app_cw, act, first, store, write_hd, alpha);
-        if (check) {
-            if (act && fail) atomicOr(&s_fail[slot], 1);
+        iterate_rows<WEIGHTED, LAYERED>(tab, s, s4old, dnew, wpair, st_base, gllr, hd_base, act, first, store,
+                                        early_stop || last, alpha);
+        if (early_stop && !last) {  // the rows ended with a barrier
+            if (act) check_rows(tab, s, s4old + dnew, hd_base, &s_fail[slot]);
             __syncthreads();
             const bool conv = act && s_fail[slot] == 0;
-            if (conv)  // HD of the previous iteration is a codeword
-                write_outputs(tab, lold, hd, 0, st_base, s, out.packed, out.app, out.iters, t, false);
+            if (conv)  // HD of this iteration is a codeword
+                write_outputs(tab, lnew, hd, 1, st_base, s, out.packed, out.app, out.iters, t + 1, true);
             slot_done = slot_done || conv;
             if (__syncthreads_and(slot_done)) break;
         }
@@ -457,7 +421,7 @@ __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slo
             if (!slot_done) write_outputs(tab, lnew, hd, 1, st_base, s, out.packed, out.app, out.iters, n_iter, true);
             break;
         }
-        if (!slot_done)  // the posterior just accumulated is the next iteration's input
+        if (!LAYERED && !slot_done)  // the posterior just accumulated is the next iteration's input
             for (int k = static_cast<int>(s); k < cf / 4; k += z)
                 reinterpret_cast<float4*>(lold)[k] = reinterpret_cast<const float4*>(lnew)[k];
     }

@@ -6,7 +6,13 @@ back.  The reference counts errors over the info bits of each codeword
 (src/encoding_tools.cpp:112-155); so does this.
 
     python -m nr_ldpc_gb300.evaluate --bg 1 --z 384 --ebn0 1.5 2.0 --iters 10 \
-        [--weights bg1_T8 --w-iters 6] [--frames 100000] [--early-stop]
+        [--weights bg1_T8] [--schedule layered] [--frames 100000] [--early-stop]
+
+    python -m nr_ldpc_gb300.evaluate --compare   # the learned-vs-plain table:
+        BG1 Z=384, batch 16384, Eb/N0 1.0..2.0 dB, early stop on: plain
+        flooding min-sum at 10 iterations, the learned layered decoder
+        (weights/bg1_L6) at 4, 5, 6 iterations, the layered decoder without
+        weights at 6, until 100 frame errors or 2^20 frames per point.
 """
 from __future__ import annotations
 
@@ -89,14 +95,40 @@ def main():
     ap.add_argument("--frames", type=int, default=65536)
     ap.add_argument("--early-stop", action="store_true")
     ap.add_argument("--weights", default=None, help="committed weight file name (weights/<name>.npy)")
+    ap.add_argument("--schedule", default="flooding", choices=["flooding", "layered"])
+    ap.add_argument("--compare", action="store_true", help="the learned-vs-plain FER table")
     args = ap.parse_args()
+    if args.compare:
+        compare()
+        return
     dec = Decoder(bg=args.bg, z=args.z, max_batch=8192)
+    dec.set_schedule(args.schedule)
     if args.weights:
         dec.set_weights(load_weights(args.weights))
     for eb in args.ebn0:
         r = measure(dec, eb, args.iters, args.frames, early_stop=args.early_stop,
                     weighted=args.weights is not None)
         print(json.dumps(r), flush=True)
+
+
+def compare(ebn0=(1.0, 1.25, 1.5, 1.6, 1.7, 1.8, 1.9, 2.0), max_frames: int = 1 << 20, min_errors: int = 100,
+            batch: int = 16384):
+    """FER of plain min-sum (flooding, 10 iterations) against the learned
+    layered decoder at 4/5/6 iterations and the layered decoder without
+    weights, early stop on; one JSON line per (decoder, Eb/N0)."""
+    dec = Decoder(bg=1, z=384, max_batch=batch)
+    configs = [("plain flooding", "flooding", None, 10), ("learned layered", "layered", "bg1_L6", 4),
+               ("learned layered", "layered", "bg1_L6", 5), ("learned layered", "layered", "bg1_L6", 6),
+               ("layered alpha 0.75", "layered", None, 6)]
+    for name, sched, weights, iters in configs:
+        dec.set_schedule(sched)
+        if weights:
+            dec.set_weights(load_weights(weights))
+        for eb in ebn0:
+            r = measure(dec, eb, iters, max_frames, batch=batch, early_stop=True, weighted=weights is not None,
+                        max_frame_errors=min_errors)
+            r.update(decoder=name, schedule=sched, weights=weights or "alpha 0.75", iters_max=iters)
+            print(json.dumps(r), flush=True)
 
 
 if __name__ == "__main__":
