@@ -12,7 +12,9 @@ the same metric through the reference-shaped host call
 ``learned_vs_plain`` (in the same line) compares the learned decoder with plain
 min-sum at a stated Eb/N0 where plain flooding at 10 iterations has FER <=
 1e-2: FER with 95% intervals over 65,536 fresh codewords and info Gbit/s of
-each (early stop on for both).
+each (early stop on for both).  ``mixed_batch`` times the uneven (BG, Z,
+rate-matched) 8192-codeword workload in one launch; ``training`` the learned
+decoder's training step (BG2 Z=128, 8 iterations, 16384 codewords).
 
 Under torchrun each rank decodes its own batch (codewords are independent:
 replicas, weak scaling); rank 0 prints one JSON line with the max time over
@@ -231,6 +233,71 @@ def learned_vs_plain(dec, stream, batch: int, ebn0: float = 1.8, frames: int = 6
     return res, launches
 
 
+def mixed_batch(stream, n: int = 8192, n_iter: int = 10, reps: int = 5):
+    """The uneven-batch workload: n codewords mixing BG1/BG2 with Z uniform in
+    {64..384}, rate-matched lengths with filler bits, Eb/N0 uniform in 1-3 dB,
+    one persistent CUDA-graph launch, early stop, at most n_iter iterations.
+    Returns info Gbit/s (sum of K' over the batch / decode time) and FER."""
+    import torch
+    from nr_ldpc_gb300.batch import Batch, make_jobs
+    rng = np.random.default_rng(2024)
+    bg = rng.integers(1, 3, n)
+    z = rng.choice((64, 96, 128, 192, 256, 320, 384), n)
+    kb = np.where(bg == 1, 22, 10)
+    kp = kb * z - rng.integers(0, 40, n)
+    e = np.maximum((kp / rng.uniform(0.25, 0.8, n)).astype(np.int64), 2 * z + 8)
+    eb = rng.uniform(1.0, 3.0, n)
+    sigma = np.sqrt((e / kp) / (2.0 * 10 ** (eb / 10))).astype(np.float32)
+    jobs, n_llr, n_e, n_out = make_jobs(bg, z, kp, e, 0, sigma)
+    b = Batch(max_jobs=n)
+    b.set_jobs(jobs)
+    llr_e = torch.empty(n_e, device="cuda")
+    cw = torch.empty(n_out, dtype=torch.uint8, device="cuda")
+    b.gen(9, 0, llr_e, cw)
+    llr = torch.empty(n_llr, device="cuda")
+    b.derate(llr_e, llr)
+    packed = torch.empty(n_out, dtype=torch.uint8, device="cuda")
+    iters = torch.empty(n, dtype=torch.int32, device="cuda")
+    for _ in range(3):
+        b.decode(llr, packed, n_iter, early_stop=True, iters=iters)
+    counts = b.count_errors(packed, cw)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        b.decode(llr, packed, n_iter, early_stop=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    info_bits = int(kp.sum())
+    res = {"codewords": n, "ms_per_batch": ms, "info_gbps": info_bits / (ms * 1e-3) / 1e9,
+           "cw_per_s": n / (ms * 1e-3), "fer": int(counts[1]) / n,
+           "avg_iters": float(iters.float().mean().item()), "launches_per_batch": 1,
+           "workload": "BG1/BG2 mix, Z in {64..384}, rate-matched with filler, Eb/N0 U[1,3] dB, "
+                       f"early stop, max {n_iter} iterations"}
+    b.close()
+    return res
+
+
+def training_step(steps: int = 5):
+    """Learned weighted min-sum training on its specified configuration:
+    BG2 Z=128, 8 unrolled iterations, 16,384 codewords per step (generation,
+    forward, adjoint, Adam all on the GPU); milliseconds per step."""
+    import torch
+    from nr_ldpc_gb300.learned import Trainer
+    tr = Trainer(bg=2, z=128, n_iter=8, batch=16384, chunk=4096, lr=1e-3, seed=5)
+    for _ in range(2):
+        tr.step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        tr.step()
+    torch.cuda.synchronize()
+    ms = 1e3 * (time.perf_counter() - t0) / steps
+    return {"config": "BG2 Z=128, 8 iterations, 16384 codewords/step, Adam 1e-3", "ms_per_step": ms,
+            "codewords_per_s": 16384 / (ms * 1e-3), "steps_timed": steps}
+
+
 def cpu_baseline(llr_host: np.ndarray, n_sample: int):
     """Reference algorithm on the host cores: the oracle's C restatement of
     the reference min-sum (kind 'port'), all cores, one codeword per thread."""
@@ -298,6 +365,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling)")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain comparison")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the mixed-batch and training legs (profiling)")
     ap.add_argument("--batch", type=int, default=BATCH,
                     help="codewords per step (profiling a smaller launch; default 4096)")
     args = ap.parse_args()
@@ -357,6 +426,8 @@ def main():
         e2e_ms = run_e2e(dec, llr, packed, args.steps, stream, world)
 
     lvp, lvp_launches = (None, 0) if args.no_learned else learned_vs_plain(dec, stream, min(B, 4096))
+    extra = {} if args.no_extra or rank != 0 else {"mixed_batch": mixed_batch(stream),
+                                                    "training": training_step()}
 
     peak, peak_kind = measured_peaks()
     bytes_launch = model_bytes_per_cw(ITERS) * B
@@ -386,6 +457,7 @@ def main():
     }
     if lvp is not None:
         line["learned_vs_plain"] = lvp
+    line.update(extra)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(llr.cpu().numpy(), n_sample=min(B, 1024))
     if rank == 0:

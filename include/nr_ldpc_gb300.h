@@ -240,6 +240,28 @@ int nrldpc_decode_noalloc(int bg, int z, float alpha, const float* d_llr, uint8_
 int nrldpc_crc(const uint8_t* d_packed, int n_cw, int stride_bytes, int n_bits, int crc_type,
                uint32_t* d_rem, nrldpc_stream_t stream);
 
+/* Code-block segmentation (3GPP TS 38.212 5.2.2) of a transport block of B
+ * bits (TB CRC included) for base graph bg: C blocks of k_prime bits each
+ * (CRC24B of L = 24 bits per block when C > 1), lifting size zc, K = kb_max*zc
+ * decoder info bits of which filler = K - k_prime are <NULL>.  B' = B + C*L
+ * must divide by C (TS 38.214's TB sizes do).  No reference counterpart: the
+ * reference computes C (src/nr_ldpc.cpp:64-81) but supports C = 1 only. */
+typedef struct {
+    int B, C, L, k_prime, k, zc, kb, filler, bg;
+} nrldpc_segment_info;
+int nrldpc_segment(int B, int bg, nrldpc_segment_info* out);
+
+/* Device side of the segmentation.  d_tb: B bits packed LSB-first.
+ * nrldpc_cb_segment writes C blocks of k_prime bits (data, then CRC24B when
+ * C > 1; bits past k_prime zero) at d_blocks + r * block_stride.
+ * nrldpc_cb_desegment is its inverse on decoded blocks: the data bits go back
+ * to d_tb, and d_crc_rem[r] (C entries, may be NULL when C = 1) is the CRC24B
+ * remainder of block r (0 = block CRC passes). */
+int nrldpc_cb_segment(const uint8_t* d_tb, const nrldpc_segment_info* info, uint8_t* d_blocks,
+                      int block_stride, nrldpc_stream_t stream);
+int nrldpc_cb_desegment(const uint8_t* d_blocks, int block_stride, const nrldpc_segment_info* info,
+                        uint8_t* d_tb, uint32_t* d_crc_rem, nrldpc_stream_t stream);
+
 /* Last device-side error recorded by a bounded wait (0 if none); clears it. */
 int nrldpc_device_error(nrldpc_handle* h);
 

@@ -35,6 +35,10 @@ class ConfigC(C.Structure):
                 ("device", C.c_int), ("cw_per_cta", C.c_int)]
 
 
+class SegmentInfoC(C.Structure):
+    _fields_ = [(n, C.c_int) for n in ("B", "C", "L", "k_prime", "k", "zc", "kb", "filler", "bg")]
+
+
 _vp, _i, _f, _u64 = C.c_void_p, C.c_int, C.c_float, C.c_uint64
 _ip = C.POINTER(C.c_int)
 
@@ -69,6 +73,9 @@ SIGNATURES = {
     "nrldpc_batch_count_errors": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "nrldpc_rm_k0": (_i, [_i, _i, _i]),
     "nrldpc_crc": (_i, [_vp, _i, _i, _i, _i, _vp, _vp]),
+    "nrldpc_segment": (_i, [_i, _i, C.POINTER(SegmentInfoC)]),
+    "nrldpc_cb_segment": (_i, [_vp, C.POINTER(SegmentInfoC), _vp, _i, _vp]),
+    "nrldpc_cb_desegment": (_i, [_vp, _i, C.POINTER(SegmentInfoC), _vp, _vp, _vp]),
     "nrldpc_decode_noalloc": (_i, [_i, _i, _f, _vp, _vp, _i, _i, _i, _vp]),
     "nrldpc_device_error": (_i, [_vp]),
     "nrldpc_status_string": (C.c_char_p, [_i]),

@@ -618,6 +618,64 @@ int nrldpc_crc(const uint8_t* d_packed, int n_cw, int stride_bytes, int n_bits, 
                                d_rem, reinterpret_cast<cudaStream_t>(stream)));
 }
 
+int nrldpc_segment(int B, int bg, nrldpc_segment_info* out) {
+    if (!out || B < 1 || (bg != 1 && bg != 2)) return NRLDPC_ERR_INVALID_ARG;
+    const int kcb = bg == 1 ? 8448 : 3840;  // maximum code block size
+    nrldpc_segment_info g{};
+    g.B = B;
+    g.bg = bg;
+    if (B <= kcb) {
+        g.L = 0;
+        g.C = 1;
+    } else {
+        g.L = 24;
+        g.C = (B + (kcb - g.L) - 1) / (kcb - g.L);
+    }
+    const long bp = static_cast<long>(B) + static_cast<long>(g.C) * g.L;
+    if (bp % g.C != 0) return NRLDPC_ERR_BAD_CONFIG;  // not a TS 38.214 transport block size
+    g.k_prime = static_cast<int>(bp / g.C);
+    if (bg == 1)
+        g.kb = 22;
+    else
+        g.kb = B > 640 ? 10 : (B > 560 ? 9 : (B > 192 ? 8 : 6));
+    int zc = 0;  // smallest lifting size of any set with kb * Z >= K'
+    for (int i = 0; i < 8; i++)
+        for (int z = kBaseZ[i]; z <= 384; z *= 2)
+            if (g.kb * z >= g.k_prime && (zc == 0 || z < zc)) zc = z;
+    if (zc == 0) return NRLDPC_ERR_BAD_CONFIG;
+    g.zc = zc;
+    g.k = (bg == 1 ? 22 : 10) * zc;
+    g.filler = g.k - g.k_prime;
+    *out = g;
+    return NRLDPC_OK;
+}
+
+int nrldpc_cb_segment(const uint8_t* d_tb, const nrldpc_segment_info* info, uint8_t* d_blocks,
+                      int block_stride, nrldpc_stream_t stream) {
+    if (!info || !d_tb || !d_blocks || info->C < 1 || info->k_prime < 1 || info->L < 0 ||
+        info->k_prime <= info->L || block_stride * 8 < info->k_prime)
+        return NRLDPC_ERR_INVALID_ARG;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const int data_bits = info->k_prime - info->L;
+    if (launch_cb_gather_blocks(d_tb, info->C, data_bits, info->k_prime, d_blocks, block_stride, st) !=
+        cudaSuccess)
+        return NRLDPC_ERR_CUDA;
+    if (info->L == 0) return NRLDPC_OK;
+    return map_cuda(launch_cb_attach_crc(d_blocks, info->C, data_bits, block_stride, 0x800063u, 24, st));
+}
+
+int nrldpc_cb_desegment(const uint8_t* d_blocks, int block_stride, const nrldpc_segment_info* info,
+                        uint8_t* d_tb, uint32_t* d_crc_rem, nrldpc_stream_t stream) {
+    if (!info || !d_tb || !d_blocks || info->C < 1 || info->k_prime < 1 || info->L < 0 ||
+        info->k_prime <= info->L || block_stride * 8 < info->k_prime || (info->L > 0 && !d_crc_rem))
+        return NRLDPC_ERR_INVALID_ARG;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (info->L > 0 &&
+        launch_crc(d_blocks, info->C, block_stride, info->k_prime, 0x800063u, 24, d_crc_rem, st) != cudaSuccess)
+        return NRLDPC_ERR_CUDA;
+    return map_cuda(launch_cb_gather_tb(d_blocks, block_stride, info->C, info->k_prime - info->L, d_tb, st));
+}
+
 int nrldpc_device_error(nrldpc_handle* handle) {
     Handle* h = reinterpret_cast<Handle*>(handle);
     if (!h) return NRLDPC_ERR_INVALID_ARG;

@@ -165,6 +165,66 @@ cudaError_t launch_dequant(const void* in, int qtype, float scale, size_t n, flo
     return cudaGetLastError();
 }
 
+// ---- code-block segmentation (TS 38.212 5.2.2) ------------------------------------
+// One thread per output byte: block r's byte j holds bits 8j..8j+7 of its
+// data, which are transport-block bits r*data_bits + 8j + i (bits at or past
+// data_bits are left zero for the CRC and the padding).
+__global__ void __launch_bounds__(256) cb_gather_blocks_kernel(const uint8_t* __restrict__ tb, int C,
+                                                               int data_bits, int k_prime,
+                                                               uint8_t* __restrict__ blocks, int stride) {
+    const int nbytes = (k_prime + 7) / 8;
+    const long idx = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x;
+    if (idx >= static_cast<long>(C) * nbytes) return;
+    const int r = static_cast<int>(idx / nbytes), j = static_cast<int>(idx - static_cast<long>(r) * nbytes);
+    uint32_t v = 0;
+    for (int i = 0; i < 8; i++) {
+        const int k = 8 * j + i;
+        if (k < data_bits) {
+            const long t = static_cast<long>(r) * data_bits + k;
+            v |= ((tb[t >> 3] >> (t & 7)) & 1u) << i;
+        }
+    }
+    blocks[static_cast<size_t>(r) * stride + j] = static_cast<uint8_t>(v);
+}
+
+// One thread per block: CRC of the data bits, appended MSB first (parity bit
+// p_0 = remainder bit len-1), so the block's remainder over all its bits is 0.
+__global__ void __launch_bounds__(128) cb_attach_crc_kernel(uint8_t* __restrict__ blocks, int C, int data_bits,
+                                                            int stride, uint32_t poly, int len) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= C) return;
+    uint8_t* p = blocks + static_cast<size_t>(r) * stride;
+    const uint32_t mask = (len >= 32) ? 0xffffffffu : ((1u << len) - 1u), top = 1u << (len - 1);
+    uint32_t rem = 0;
+    for (int i = 0; i < data_bits; i++) {
+        const uint32_t fb = ((rem & top) != 0) ^ ((p[i >> 3] >> (i & 7)) & 1u);
+        rem = (rem << 1) & mask;
+        if (fb) rem ^= poly;
+    }
+    for (int i = 0; i < len; i++) {
+        const int k = data_bits + i;
+        const uint32_t bit = (rem >> (len - 1 - i)) & 1u;
+        p[k >> 3] = static_cast<uint8_t>((p[k >> 3] & ~(1u << (k & 7))) | (bit << (k & 7)));
+    }
+}
+
+// One thread per transport-block byte: bit t comes from block t / data_bits.
+__global__ void __launch_bounds__(256) cb_gather_tb_kernel(const uint8_t* __restrict__ blocks, int stride, int C,
+                                                           int data_bits, uint8_t* __restrict__ tb) {
+    const long total = static_cast<long>(C) * data_bits;
+    const long j = blockIdx.x * static_cast<long>(blockDim.x) + threadIdx.x;
+    if (j >= (total + 7) / 8) return;
+    uint32_t v = 0;
+    for (int i = 0; i < 8; i++) {
+        const long t = 8 * j + i;
+        if (t < total) {
+            const int r = static_cast<int>(t / data_bits), k = static_cast<int>(t - static_cast<long>(r) * data_bits);
+            v |= ((blocks[static_cast<size_t>(r) * stride + (k >> 3)] >> (k & 7)) & 1u) << i;
+        }
+    }
+    tb[j] = static_cast<uint8_t>(v);
+}
+
 cudaError_t launch_crc(const uint8_t* packed, int n_cw, int stride, int n_bits, uint32_t poly, int len,
                        uint32_t* rem, cudaStream_t stream) {
     crc_kernel<<<(n_cw + 255) / 256, 256, 0, stream>>>(packed, n_cw, stride, n_bits, poly, len, rem);
@@ -254,4 +314,25 @@ cudaError_t launch_count_errors(const uint8_t* packed, const uint8_t* cw_packed,
     return cudaGetLastError();
 }
 
+}  // namespace nrldpc
+
+namespace nrldpc {
+cudaError_t launch_cb_gather_blocks(const uint8_t* tb, int C, int data_bits, int k_prime, uint8_t* blocks,
+                                    int stride, cudaStream_t stream) {
+    const long n = static_cast<long>(C) * ((k_prime + 7) / 8);
+    cb_gather_blocks_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, stream>>>(tb, C, data_bits, k_prime,
+                                                                                         blocks, stride);
+    return cudaGetLastError();
+}
+cudaError_t launch_cb_attach_crc(uint8_t* blocks, int C, int data_bits, int stride, uint32_t poly, int len,
+                                 cudaStream_t stream) {
+    cb_attach_crc_kernel<<<(C + 127) / 128, 128, 0, stream>>>(blocks, C, data_bits, stride, poly, len);
+    return cudaGetLastError();
+}
+cudaError_t launch_cb_gather_tb(const uint8_t* blocks, int stride, int C, int data_bits, uint8_t* tb,
+                                cudaStream_t stream) {
+    const long n = (static_cast<long>(C) * data_bits + 7) / 8;
+    cb_gather_tb_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, stream>>>(blocks, stride, C, data_bits, tb);
+    return cudaGetLastError();
+}
 }  // namespace nrldpc

@@ -137,6 +137,15 @@ cudaError_t launch_dequant(const void* in, int qtype, float scale, size_t n, flo
                            cudaStream_t stream);
 cudaError_t launch_crc(const uint8_t* packed, int n_cw, int stride, int n_bits, uint32_t poly, int len,
                        uint32_t* rem, cudaStream_t stream);
+// Code-block segmentation (channel.cu): bit gathers between a transport
+// block and C code blocks of k_prime bits (data_bits = k_prime - L each), and
+// CRC attachment of the last L bits of each block.
+cudaError_t launch_cb_gather_blocks(const uint8_t* tb, int C, int data_bits, int k_prime, uint8_t* blocks,
+                                    int stride, cudaStream_t stream);
+cudaError_t launch_cb_attach_crc(uint8_t* blocks, int C, int data_bits, int stride, uint32_t poly, int len,
+                                 cudaStream_t stream);
+cudaError_t launch_cb_gather_tb(const uint8_t* blocks, int stride, int C, int data_bits, uint8_t* tb,
+                                cudaStream_t stream);
 cudaError_t launch_count_errors(const uint8_t* packed, const uint8_t* cw_packed, int n_cw,
                                 int packed_bytes, int n_info, unsigned long long* counts,
                                 cudaStream_t stream);

@@ -309,3 +309,42 @@ class RefEmu:
         if rc:
             raise RuntimeError(f"ref_transmit_llr rc={rc}")
         return llr, info
+
+
+# ---- code-block segmentation (3GPP TS 38.212 5.2.2), restated -----------------------
+LIFTING_SIZES = sorted({a << j for a in (2, 3, 5, 7, 9, 11, 13, 15) for j in range(8) if a << j <= 384})
+
+
+def segment_info(B: int, bg: int) -> dict:
+    """C, L, K', K, Zc, Kb and filler count for a B-bit transport block (its
+    CRC included); None when B + C*L does not divide by C."""
+    kcb = 8448 if bg == 1 else 3840
+    if B <= kcb:
+        L, Cn = 0, 1
+    else:
+        L = 24
+        Cn = -(-B // (kcb - L))
+    if (B + Cn * L) % Cn:
+        return None
+    kp = (B + Cn * L) // Cn
+    if bg == 1:
+        kb = 22
+    else:
+        kb = 10 if B > 640 else 9 if B > 560 else 8 if B > 192 else 6
+    zc = min(z for z in LIFTING_SIZES if kb * z >= kp)
+    k = (22 if bg == 1 else 10) * zc
+    return {"B": B, "C": Cn, "L": L, "k_prime": kp, "k": k, "zc": zc, "kb": kb, "filler": k - kp, "bg": bg}
+
+
+def cb_segment(tb_bits: np.ndarray, info: dict) -> np.ndarray:
+    """[C, K'] bits of the code blocks: consecutive TB bits, then CRC24B (MSB
+    first) when C > 1."""
+    Cn, L, kp = info["C"], info["L"], info["k_prime"]
+    d = kp - L
+    out = np.zeros((Cn, kp), np.uint8)
+    for r in range(Cn):
+        out[r, :d] = tb_bits[r * d:(r + 1) * d]
+        if L:
+            rem = crc(np.packbits(out[r, :d], bitorder="little"), d, CRC24B)
+            out[r, d:] = [(rem >> (L - 1 - i)) & 1 for i in range(L)]
+    return out
