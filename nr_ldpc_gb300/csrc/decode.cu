@@ -167,11 +167,12 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
             mag = __fmul_rn(wpair[e0 + i].x, i == oidx ? om2 : om1);
         else
             mag = i == oidx ? oa2 : oa1;
-        const float ro = __uint_as_float(__float_as_uint(mag) | ((oinfo << (23 - i)) & 0x80000000u));
+        const float ro = __uint_as_float(__float_as_uint(mag) | ((oinfo << (24 - D + i)) & 0x80000000u));
         const float q = __fsub_rn(lv[i], ro);
         keep[i] = LAYERED ? q : ro;
         const float qa = fabsf(q);
-        if (q < 0.0f) qmask |= 1u << i;
+        // sign bit of q + 0 is (q < 0): -0 becomes +0, NaN results are canonical (+)
+        qmask = __funnelshift_l(__float_as_uint(__fadd_rn(q, 0.0f)), qmask, 1);  // edge i at bit D-1-i
         if (qa < m1) idx = i;
         const float mx = max_nan(m1, qa);  // NaN |Q| leaves min1/min2 untouched
         m1 = fminf(m1, qa);
@@ -193,7 +194,7 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
                 mag = __fmul_rn(wpair[e0 + i].y, i == idx ? m2 : m1);
             else
                 mag = i == idx ? a2 : a1;
-            const float rn = __uint_as_float(__float_as_uint(mag) | ((rsign << (31 - i)) & 0x80000000u));
+            const float rn = __uint_as_float(__float_as_uint(mag) | ((rsign << (32 - D + i)) & 0x80000000u));
             const float v = __fadd_rn(keep[i], rn);
             if (i == LAST && sfx)
                 sfx_new = v;
@@ -215,7 +216,7 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
                 mag = __fmul_rn(wpair[e0 + i].y, i == idx ? m2 : m1);
             else
                 mag = i == idx ? a2 : a1;
-            const float rn = __uint_as_float(__float_as_uint(mag) | ((rsign << (31 - i)) & 0x80000000u));
+            const float rn = __uint_as_float(__float_as_uint(mag) | ((rsign << (32 - D + i)) & 0x80000000u));
             const float dt = __fsub_rn(rn, keep[i]);
             const float v = __fadd_rn(nv[i], dt);
             if (i == LAST && sfx)
