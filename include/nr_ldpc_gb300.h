@@ -120,7 +120,8 @@ int nrldpc_decode_host_async_q(nrldpc_handle* h, const void* h_llr_q, int qtype,
 
 /* Learned weighted min-sum: per (iteration, base edge) scale factors
  * w[n_w_iters][n_edges] replacing alpha (iterations past n_w_iters reuse the
- * last row).  Host pointer; copied into the handle.  n_w_iters = 0 clears. */
+ * last row; n_w_iters <= 16, else NRLDPC_ERR_TOO_LARGE).  Host pointer; copied
+ * into the handle.  n_w_iters = 0 clears. */
 int nrldpc_set_weights(nrldpc_handle* h, const float* w, int n_w_iters);
 /* As nrldpc_decode, with the weights set on the handle. */
 int nrldpc_decode_weighted(nrldpc_handle* h, const float* d_llr, uint8_t* d_packed, int n_cw,

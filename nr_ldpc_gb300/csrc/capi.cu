@@ -35,7 +35,7 @@ struct Handle {
     float* stage_llr = nullptr;
     uint8_t* stage_packed = nullptr;
     void* stage_q = nullptr;  // fp16 / int8 LLR staging (nrldpc_decode_host_async_q)
-    float* weights = nullptr;
+    WeightTable* weights = nullptr;  // host copy, passed by value to the weighted kernels
     int n_w_iters = 0;
     bool wms_ready = false;
     int schedule = NRLDPC_SCHEDULE_FLOODING;
@@ -136,7 +136,7 @@ void free_handle(Handle* h) {
     cudaFree(h->stage_llr);
     cudaFree(h->stage_packed);
     cudaFree(h->stage_q);
-    cudaFree(h->weights);
+    delete h->weights;
     for (cudaEvent_t e : h->ev_chunk)
         if (e) cudaEventDestroy(e);
     if (h->ev_start) cudaEventDestroy(h->ev_start);
@@ -234,7 +234,6 @@ int decode_impl(Handle* h, const float* llr, uint8_t* packed, int n_cw, int n_it
     a.state = h->state;
     a.work_counter = h->scratch;
     a.error_flag = h->scratch + 1;
-    a.weights = weighted ? h->weights : nullptr;
     a.n_cw = n_cw;
     a.n_iter = n_iter;
     a.cpb = h->cpb;
@@ -245,7 +244,7 @@ int decode_impl(Handle* h, const float* llr, uint8_t* packed, int n_cw, int n_it
     const int grid = std::min(a.n_groups, h->max_grid);
     cudaError_t e = cudaMemsetAsync(h->scratch, 0, sizeof(int), stream);
     if (e != cudaSuccess) return NRLDPC_ERR_CUDA;
-    return map_cuda(launch_decode(h->tab, a, grid, h->threads, h->smem, weighted,
+    return map_cuda(launch_decode(h->tab, a, weighted ? h->weights : nullptr, grid, h->threads, h->smem,
                                   h->schedule == NRLDPC_SCHEDULE_LAYERED, h->minb, stream));
 }
 
@@ -480,13 +479,16 @@ int nrldpc_set_schedule(nrldpc_handle* handle, int schedule) {
 int nrldpc_set_weights(nrldpc_handle* handle, const float* w, int n_w_iters) {
     Handle* h = reinterpret_cast<Handle*>(handle);
     if (!h || n_w_iters < 0 || (n_w_iters > 0 && !w)) return NRLDPC_ERR_INVALID_ARG;
-    cudaFree(h->weights);
+    if (n_w_iters > kMaxWIters) return NRLDPC_ERR_TOO_LARGE;
+    delete h->weights;
     h->weights = nullptr;
     h->n_w_iters = 0;
     if (n_w_iters == 0) return NRLDPC_OK;
-    const size_t bytes = static_cast<size_t>(n_w_iters) * h->tab.n_edges * sizeof(float);
-    if (cudaMalloc(&h->weights, bytes) != cudaSuccess) return NRLDPC_ERR_NO_MEMORY;
-    if (cudaMemcpy(h->weights, w, bytes, cudaMemcpyHostToDevice) != cudaSuccess) return NRLDPC_ERR_CUDA;
+    h->weights = new (std::nothrow) WeightTable();  // zero-initialised, incl. the zero row
+    if (!h->weights) return NRLDPC_ERR_NO_MEMORY;
+    for (int t = 0; t < n_w_iters; t++)
+        std::memcpy(h->weights->w[t], w + static_cast<size_t>(t) * h->tab.n_edges,
+                    sizeof(float) * h->tab.n_edges);
     h->n_w_iters = n_w_iters;
     return NRLDPC_OK;
 }

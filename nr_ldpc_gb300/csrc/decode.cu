@@ -129,8 +129,8 @@ __device__ __forceinline__ uint32_t lds_u8(uint32_t a) {
 template <int D, bool WEIGHTED, bool LAYERED>
 __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sfx, uint32_t s,
                                            uint32_t s4old, uint32_t dnew, uint32_t z4,
-                                           const float2* wpair, uint4 st, uint4* st_out, uint32_t hd,
-                                           float alpha) {
+                                           const float* wprev, const float* wcur, uint4 st, uint4* st_out,
+                                           uint32_t hd, float alpha) {
     constexpr int LAST = D - 1;
     uint32_t addr[D];
     float lv[D];
@@ -164,7 +164,7 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
     for (int i = 0; i < D; i++) {
         float mag;
         if (WEIGHTED)
-            mag = __fmul_rn(wpair[e0 + i].x, i == oidx ? om2 : om1);
+            mag = __fmul_rn(wprev[e0 + i], i == oidx ? om2 : om1);
         else
             mag = i == oidx ? oa2 : oa1;
         const float ro = __uint_as_float(__float_as_uint(mag) | ((oinfo << (24 - D + i)) & 0x80000000u));
@@ -191,7 +191,7 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
         for (int i = 0; i < D; i++) {
             float mag;
             if (WEIGHTED)
-                mag = __fmul_rn(wpair[e0 + i].y, i == idx ? m2 : m1);
+                mag = __fmul_rn(wcur[e0 + i], i == idx ? m2 : m1);
             else
                 mag = i == idx ? a2 : a1;
             const float rn = __uint_as_float(__float_as_uint(mag) | ((rsign << (32 - D + i)) & 0x80000000u));
@@ -213,7 +213,7 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
             if (i + kPipe < D) nv[i + kPipe] = (i + kPipe == LAST && sfx) ? lv[i + kPipe] : lds(addr[i + kPipe] + dnew);
             float mag;
             if (WEIGHTED)
-                mag = __fmul_rn(wpair[e0 + i].y, i == idx ? m2 : m1);
+                mag = __fmul_rn(wcur[e0 + i], i == idx ? m2 : m1);
             else
                 mag = i == idx ? a2 : a1;
             const float rn = __uint_as_float(__float_as_uint(mag) | ((rsign << (32 - D + i)) & 0x80000000u));
@@ -235,12 +235,12 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
 template <bool WEIGHTED, bool LAYERED>
 __device__ __forceinline__ void row_dispatch(int deg, const CodeTable& tab, int e0, bool sfx, uint32_t s,
                                              uint32_t s4old, uint32_t dnew, uint32_t z4,
-                                             const float2* wpair, uint4 st, uint4* st_out, uint32_t hd,
-                                             float alpha) {
+                                             const float* wprev, const float* wcur, uint4 st, uint4* st_out,
+                                             uint32_t hd, float alpha) {
     switch (deg) {
 #define NRLDPC_ROW_CASE(D)                                                                         \
     case D:                                                                                        \
-        row_update<D, WEIGHTED, LAYERED>(tab, e0, sfx, s, s4old, dnew, z4, wpair, st, st_out, hd, \
+        row_update<D, WEIGHTED, LAYERED>(tab, e0, sfx, s, s4old, dnew, z4, wprev, wcur, st, st_out, hd, \
                                          alpha);                                                  \
         break;
         NRLDPC_ROW_CASE(1) NRLDPC_ROW_CASE(2) NRLDPC_ROW_CASE(3) NRLDPC_ROW_CASE(4)
@@ -311,7 +311,8 @@ __device__ __forceinline__ void write_outputs(const CodeTable& tab, const float*
 //   decisions.
 template <bool WEIGHTED, bool LAYERED>
 __device__ __forceinline__ void iterate_rows(const CodeTable& tab, uint32_t s, uint32_t s4old, uint32_t dnew,
-                                             const float2* wpair, uint4* st_base, const float* gllr,
+                                             const float* wprev, const float* wcur, uint4* st_base,
+                                             const float* gllr,
                                              uint32_t hd_base, bool act, bool first, bool store, bool write_hd,
                                              float alpha) {
     const int z = tab.z, rows = tab.rows;
@@ -328,7 +329,7 @@ __device__ __forceinline__ void iterate_rows(const CodeTable& tab, uint32_t s, u
         const uint4 s2 = fetch(r + 2);
         if (act) {
             const bool sfx = tab.row_sfx[r] != 0;
-            row_dispatch<WEIGHTED, LAYERED>(tab.row_deg[r], tab, tab.row_ptr[r], sfx, s, s4old, dnew, z4, wpair,
+            row_dispatch<WEIGHTED, LAYERED>(tab.row_deg[r], tab, tab.row_ptr[r], sfx, s, s4old, dnew, z4, wprev, wcur,
                                             s0, store ? st_base + r * z + s : nullptr,
                                             (write_hd && sfx) ? hd_base + static_cast<uint32_t>(r * z) : 0u,
                                             alpha);
@@ -381,9 +382,9 @@ struct SlotOut {
 // oracle's rule, ldpc_oracle.c decode_one_f32).
 template <bool WEIGHTED, bool LAYERED>
 __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slot, uint32_t s,
-                                          bool slot_done, float* buf0, uint8_t* hd0, float2* wpair,
+                                          bool slot_done, float* buf0, uint8_t* hd0,
                                           int* s_fail, uint4* st_base, const float* gllr, SlotOut out,
-                                          int n_iter, int early_stop, float alpha, const float* weights,
+                                          int n_iter, int early_stop, float alpha, const float* wtab,
                                           int n_w_iters) {
     const int z = tab.z, cf = tab.core_floats, tid = threadIdx.x;
     float* lold = buf0 + static_cast<size_t>(slot) * cf;  // read by the check-node pass
@@ -397,17 +398,19 @@ __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slo
             reinterpret_cast<float4*>(lnew)[k] = reinterpret_cast<const float4*>(lold)[k];
     for (int t = 0; t < n_iter; t++) {
         const bool first = t == 0, last = t == n_iter - 1;
+        // weight rows in parameter space (uniform constant-cache reads); the
+        // zero row at t = 0, where there is no previous R
+        const float* wprev = nullptr;
+        const float* wcur = nullptr;
         if (WEIGHTED) {
-            const int tp = min(max(t - 1, 0), n_w_iters - 1), tc = min(t, n_w_iters - 1);
-            for (int e = tid; e < tab.n_edges; e += blockDim.x)  // no previous R at t = 0
-                wpair[e] = make_float2(first ? 0.0f : weights[tp * tab.n_edges + e],
-                                       weights[tc * tab.n_edges + e]);
+            wprev = wtab + (first ? kMaxWIters : min(t - 1, n_w_iters - 1)) * kMaxEdges;
+            wcur = wtab + min(t, n_w_iters - 1) * kMaxEdges;
         }
         if (tid < cpb) s_fail[tid] = 0;
         __syncthreads();
         const bool act = !slot_done;
         const bool store = !last || out.app != nullptr;
-        iterate_rows<WEIGHTED, LAYERED>(tab, s, s4old, dnew, wpair, st_base, gllr, hd_base, act, first, store,
+        iterate_rows<WEIGHTED, LAYERED>(tab, s, s4old, dnew, wprev, wcur, st_base, gllr, hd_base, act, first, store,
                                         early_stop || last, alpha);
         if (early_stop && !last) {  // the rows ended with a barrier
             if (act) check_rows(tab, s, s4old + dnew, hd_base, &s_fail[slot]);
@@ -431,15 +434,26 @@ __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slo
 
 // MINB = CTAs per SM the register budget is sized for: 1 when shared memory
 // admits a single CTA per SM anyway (BG1 Z=384), 2 otherwise.
+template <bool W>
+struct WeightParam {
+    using type = NoWeights;
+};
+template <>
+struct WeightParam<true> {
+    using type = WeightTable;
+};
+
 template <bool WEIGHTED, int MINB, bool LAYERED>
 __global__ void __launch_bounds__(kMaxThreads, MINB)
-    decode_kernel(const __grid_constant__ CodeTable tab, const __grid_constant__ DecodeArgs a) {
+    decode_kernel(const __grid_constant__ CodeTable tab, const __grid_constant__ DecodeArgs a,
+                  const __grid_constant__ typename WeightParam<WEIGHTED>::type wt) {
     extern __shared__ __align__(128) unsigned char smem[];
     const uint32_t bar = smem_addr(smem);
     int* s_group = reinterpret_cast<int*>(smem + 8);
     int* s_fail = reinterpret_cast<int*>(smem + 16);
-    float2* wpair = reinterpret_cast<float2*>(smem + kHeaderBytes);
-    float* buf0 = reinterpret_cast<float*>(smem + kHeaderBytes + kMaxEdges * 8);
+    float* buf0 = reinterpret_cast<float*>(smem + kHeaderBytes);
+    const float* wtab = nullptr;
+    if constexpr (WEIGHTED) wtab = &wt.w[0][0];
 
     const int z = tab.z, n = tab.n_bp, cpb = a.cpb, rows = tab.rows, cf = tab.core_floats;
     uint8_t* hd0 = reinterpret_cast<uint8_t*>(buf0 + 2 * static_cast<size_t>(cpb) * cf);
@@ -482,8 +496,8 @@ __global__ void __launch_bounds__(kMaxThreads, MINB)
         const size_t cw = static_cast<size_t>(cw0 + (slot_done ? 0 : slot));
         SlotOut out{a.packed + cw * tab.packed_bytes, a.app ? a.app + cw * n : nullptr,
                     a.iters ? a.iters + cw : nullptr};
-        run_group<WEIGHTED, LAYERED>(tab, cpb, slot, s, slot_done, buf0, hd0, wpair, s_fail, st_base, a.llr + cw * n, out,
-                            a.n_iter, a.early_stop, a.alpha, a.weights, a.n_w_iters);
+        run_group<WEIGHTED, LAYERED>(tab, cpb, slot, s, slot_done, buf0, hd0, s_fail, st_base, a.llr + cw * n, out,
+                                     a.n_iter, a.early_stop, a.alpha, wtab, a.n_w_iters);
     }
 }
 
@@ -544,7 +558,7 @@ __global__ void __launch_bounds__(kMaxThreads, 2)
         SlotOut out{a.packed + job.out_offset, nullptr, a.iters ? a.iters + jidx : nullptr};
         uint4* st_base = reinterpret_cast<uint4*>(a.state + static_cast<size_t>(blockIdx.x) * a.slot_words) +
                          static_cast<size_t>(valid_thread ? slot : 0) * tab.rows * z;
-        run_group<false, false>(tab, cpb, slot, s, !valid_thread, buf0, hd0, nullptr, s_fail, st_base,
+        run_group<false, false>(tab, cpb, slot, s, !valid_thread, buf0, hd0, s_fail, st_base,
                          a.llr + job.llr_offset, out, a.n_iter, a.early_stop, a.alpha, nullptr, 1);
     }
 }
@@ -552,7 +566,7 @@ __global__ void __launch_bounds__(kMaxThreads, 2)
 }  // namespace
 
 size_t decode_smem_bytes(const CodeTable& tab, int cpb) {
-    return kHeaderBytes + static_cast<size_t>(kMaxEdges) * 8 + group_smem_bytes(tab, cpb);
+    return kHeaderBytes + group_smem_bytes(tab, cpb);
 }
 
 template <bool W, int MINB, bool LAY>
@@ -604,11 +618,14 @@ int decode_max_ctas_per_sm(bool weighted, int minb, int threads, size_t smem) {
     return n;
 }
 
-cudaError_t launch_decode(const CodeTable& tab, const DecodeArgs& args, int grid, int threads,
-                          size_t smem, bool weighted, bool layered, int minb, cudaStream_t stream) {
+cudaError_t launch_decode(const CodeTable& tab, const DecodeArgs& args, const WeightTable* weights, int grid,
+                          int threads, size_t smem, bool layered, int minb, cudaStream_t stream) {
     if (args.cpb < 1 || args.cpb > kMaxCpb) return cudaErrorInvalidValue;
+    const bool weighted = weights != nullptr;
     const void* k = select_kernel(weighted, minb, layered);
-    void* params[2] = {const_cast<CodeTable*>(&tab), const_cast<DecodeArgs*>(&args)};
+    NoWeights none{};
+    void* params[3] = {const_cast<CodeTable*>(&tab), const_cast<DecodeArgs*>(&args),
+                       weighted ? const_cast<WeightTable*>(weights) : static_cast<void*>(&none)};
     return cudaLaunchKernel(k, dim3(grid), dim3(threads), params, smem, stream);
 }
 

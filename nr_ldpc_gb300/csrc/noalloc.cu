@@ -127,6 +127,6 @@ extern "C" int nrldpc_decode_noalloc(int bg, int z, float alpha, const float* d_
     const int grid = static_cast<int>(std::min<long>(a.n_groups, max_grid));
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     if (cudaMemsetAsync(s->counters, 0, 2 * sizeof(int), st) != cudaSuccess) return NRLDPC_ERR_CUDA;
-    return launch_decode(tab, a, grid, threads, smem, false, false, minb, st) == cudaSuccess ? NRLDPC_OK
+    return launch_decode(tab, a, nullptr, grid, threads, smem, false, minb, st) == cudaSuccess ? NRLDPC_OK
                                                                                        : NRLDPC_ERR_CUDA;
 }

@@ -50,6 +50,17 @@ struct alignas(16) CodeTable {
 // info = idx (bits 0..4) | R sign of edge i at bit 8+i, and the posterior of
 // the row's suffix column at this sub-row (unused in rows without one).
 constexpr size_t kStateBytesPerRow = 16;
+// Learned weights of the weighted decoder, passed by value as a kernel
+// parameter (constant bank: every lane of a warp reads the same edge's
+// weight).  Rows t < n_w_iters hold w[t][e]; row kMaxWIters stays zero (no
+// previous message in the first iteration).
+constexpr int kMaxWIters = 16;
+struct alignas(16) WeightTable {
+    float w[kMaxWIters + 1][kMaxEdges];
+};
+struct NoWeights {
+    int unused;
+};
 struct DecodeArgs {
     const float* llr;
     uint8_t* packed;
@@ -58,7 +69,6 @@ struct DecodeArgs {
     uint32_t* state;        // [grid * cpb][rows * Z][4]
     int* work_counter;      // dynamic codeword-group scheduler, zeroed per launch
     int* error_flag;        // bounded-wait failures
-    const float* weights;   // [n_w_iters][n_edges] or null
     int n_cw, n_iter, cpb, n_groups, n_w_iters, early_stop;
     float alpha;
 };
@@ -102,9 +112,10 @@ const void* batch_decode_kernel_ptr();
 
 // Host-side launchers (decode.cu / channel.cu).
 // minb: CTAs per SM the kernel's register budget assumes (1 or 2).
-// layered: row-sequential schedule (no reference counterpart) instead of flooding.
-cudaError_t launch_decode(const CodeTable& tab, const DecodeArgs& args, int grid, int threads,
-                          size_t smem, bool weighted, bool layered, int minb, cudaStream_t stream);
+// weights: null for the plain decoder; layered: row-sequential schedule (no
+// reference counterpart) instead of flooding.
+cudaError_t launch_decode(const CodeTable& tab, const DecodeArgs& args, const WeightTable* weights, int grid,
+                          int threads, size_t smem, bool layered, int minb, cudaStream_t stream);
 size_t decode_smem_bytes(const CodeTable& tab, int cpb);
 cudaError_t decode_kernel_attributes(size_t smem);
 int decode_max_ctas_per_sm(bool weighted, int minb, int threads, size_t smem);
