@@ -58,16 +58,16 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def traffic_per_cw():
-    """DRAM bytes per codeword of the decode kernel from the committed ncu
-    summary (dram__bytes_read.sum + dram__bytes_write.sum of one launch,
-    divided by the codewords that launch decoded)."""
+def ncu_summary():
+    """From the committed ncu summary of the decode kernel: DRAM bytes per
+    codeword (dram__bytes_read.sum + dram__bytes_write.sum of one launch over
+    the codewords it decoded) and SM issue utilisation."""
     p = os.path.join(ROOT, "profiles", "decode_bg1_z384_dram.json")
     if not os.path.exists(p):
-        return None
+        return None, None
     with open(p) as f:
         d = json.load(f)
-    return float(d["dram_bytes_per_cw"])
+    return float(d["dram_bytes_per_cw"]), d.get("sm_issue_active_pct")
 
 
 class ClockSampler:
@@ -432,7 +432,7 @@ def main():
     peak, peak_kind = measured_peaks()
     bytes_launch = model_bytes_per_cw(ITERS) * B
     achieved = bytes_launch / (ms_launch * 1e-3) / 1e9
-    tpc = traffic_per_cw()
+    tpc, issue_pct = ncu_summary()
     line = {
         "metric": METRIC, "value": value, "unit": "Gbit/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -451,7 +451,10 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "traffic": None if tpc is None else tpc * B,
-                     "model_bytes_per_launch": bytes_launch, "kernel_ms": ms_launch},
+                     "model_bytes_per_launch": bytes_launch, "kernel_ms": ms_launch,
+                     "sm_issue_active_pct_ncu": issue_pct,
+                     "note": "model bytes (every lifted edge message and posterior in fp32 per iteration); "
+                             "the kernel keeps them on chip and in L2 and is bound by SM issue"},
         "clocks": clocks,
         "gpu_launches": args.steps,
     }
