@@ -38,6 +38,18 @@ namespace {
 
 constexpr int kMaxCpb = 48;
 constexpr int kHeaderBytes = 1024;  // mbarrier, group id, per-slot flags
+// Weights of the current iteration in shared memory, one padded row of
+// kWPad floats per base row (previous-iteration row block, then current), so
+// a row's weights come in with 128-bit loads: [2][kMaxRows][kWPad].
+constexpr int kWPad = 20;
+constexpr int kWeightBytes = 2 * kMaxRows * kWPad * 4;
+
+// Weight i of a padded row held as float4s (i is constant after unrolling).
+__device__ __forceinline__ float wsel(const float4* w, int i) {
+    const float4 v = w[i >> 2];
+    const int c = i & 3;
+    return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w;
+}
 constexpr long kWaitLimit = 1L << 20;
 
 __device__ __forceinline__ float max_nan(float a, float b) {
@@ -129,7 +141,7 @@ __device__ __forceinline__ uint32_t lds_u8(uint32_t a) {
 template <int D, bool WEIGHTED, bool LAYERED>
 __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sfx, uint32_t s,
                                            uint32_t s4old, uint32_t dnew, uint32_t z4,
-                                           const float* wprev, const float* wcur, uint4 st, uint4* st_out,
+                                           const float4* wprev, const float4* wcur, uint4 st, uint4* st_out,
                                            uint32_t hd, float alpha) {
     constexpr int LAST = D - 1;
     uint32_t addr[D];
@@ -164,7 +176,7 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
     for (int i = 0; i < D; i++) {
         float mag;
         if (WEIGHTED)
-            mag = __fmul_rn(wprev[e0 + i], i == oidx ? om2 : om1);
+            mag = __fmul_rn(wsel(wprev, i), i == oidx ? om2 : om1);
         else
             mag = i == oidx ? oa2 : oa1;
         const float ro = __uint_as_float(__float_as_uint(mag) | ((oinfo << (24 - D + i)) & 0x80000000u));
@@ -191,7 +203,7 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
         for (int i = 0; i < D; i++) {
             float mag;
             if (WEIGHTED)
-                mag = __fmul_rn(wcur[e0 + i], i == idx ? m2 : m1);
+                mag = __fmul_rn(wsel(wcur, i), i == idx ? m2 : m1);
             else
                 mag = i == idx ? a2 : a1;
             const float rn = __uint_as_float(__float_as_uint(mag) | ((rsign << (32 - D + i)) & 0x80000000u));
@@ -213,7 +225,7 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
             if (i + kPipe < D) nv[i + kPipe] = (i + kPipe == LAST && sfx) ? lv[i + kPipe] : lds(addr[i + kPipe] + dnew);
             float mag;
             if (WEIGHTED)
-                mag = __fmul_rn(wcur[e0 + i], i == idx ? m2 : m1);
+                mag = __fmul_rn(wsel(wcur, i), i == idx ? m2 : m1);
             else
                 mag = i == idx ? a2 : a1;
             const float rn = __uint_as_float(__float_as_uint(mag) | ((rsign << (32 - D + i)) & 0x80000000u));
@@ -235,7 +247,7 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
 template <bool WEIGHTED, bool LAYERED>
 __device__ __forceinline__ void row_dispatch(int deg, const CodeTable& tab, int e0, bool sfx, uint32_t s,
                                              uint32_t s4old, uint32_t dnew, uint32_t z4,
-                                             const float* wprev, const float* wcur, uint4 st, uint4* st_out,
+                                             const float4* wprev, const float4* wcur, uint4 st, uint4* st_out,
                                              uint32_t hd, float alpha) {
     switch (deg) {
 #define NRLDPC_ROW_CASE(D)                                                                         \
@@ -311,7 +323,7 @@ __device__ __forceinline__ void write_outputs(const CodeTable& tab, const float*
 //   decisions.
 template <bool WEIGHTED, bool LAYERED>
 __device__ __forceinline__ void iterate_rows(const CodeTable& tab, uint32_t s, uint32_t s4old, uint32_t dnew,
-                                             const float* wprev, const float* wcur, uint4* st_base,
+                                             const float4* wpad, uint4* st_base,
                                              const float* gllr,
                                              uint32_t hd_base, bool act, bool first, bool store, bool write_hd,
                                              float alpha) {
@@ -329,7 +341,8 @@ __device__ __forceinline__ void iterate_rows(const CodeTable& tab, uint32_t s, u
         const uint4 s2 = fetch(r + 2);
         if (act) {
             const bool sfx = tab.row_sfx[r] != 0;
-            row_dispatch<WEIGHTED, LAYERED>(tab.row_deg[r], tab, tab.row_ptr[r], sfx, s, s4old, dnew, z4, wprev, wcur,
+            row_dispatch<WEIGHTED, LAYERED>(tab.row_deg[r], tab, tab.row_ptr[r], sfx, s, s4old, dnew, z4,
+                                            wpad + r * (kWPad / 4), wpad + (kMaxRows + r) * (kWPad / 4),
                                             s0, store ? st_base + r * z + s : nullptr,
                                             (write_hd && sfx) ? hd_base + static_cast<uint32_t>(r * z) : 0u,
                                             alpha);
@@ -384,7 +397,7 @@ template <bool WEIGHTED, bool LAYERED>
 __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slot, uint32_t s,
                                           bool slot_done, float* buf0, uint8_t* hd0,
                                           int* s_fail, uint4* st_base, const float* gllr, SlotOut out,
-                                          int n_iter, int early_stop, float alpha, const float* wtab,
+                                          int n_iter, int early_stop, float alpha, const float* wtab, float4* wpad,
                                           int n_w_iters) {
     const int z = tab.z, cf = tab.core_floats, tid = threadIdx.x;
     float* lold = buf0 + static_cast<size_t>(slot) * cf;  // read by the check-node pass
@@ -400,17 +413,24 @@ __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slo
         const bool first = t == 0, last = t == n_iter - 1;
         // weight rows in parameter space (uniform constant-cache reads); the
         // zero row at t = 0, where there is no previous R
-        const float* wprev = nullptr;
-        const float* wcur = nullptr;
-        if (WEIGHTED) {
-            wprev = wtab + (first ? kMaxWIters : min(t - 1, n_w_iters - 1)) * kMaxEdges;
-            wcur = wtab + min(t, n_w_iters - 1) * kMaxEdges;
+        if (WEIGHTED) {  // this iteration's weights into shared memory, padded per base row
+            const float* wprev = wtab + (first ? kMaxWIters : min(t - 1, n_w_iters - 1)) * kMaxEdges;
+            const float* wcur = wtab + min(t, n_w_iters - 1) * kMaxEdges;
+            float* wp = reinterpret_cast<float*>(wpad);
+            for (int k = tid; k < 2 * kMaxRows * kWPad; k += blockDim.x) {
+                const int half = k >= kMaxRows * kWPad ? 1 : 0;
+                const int rem = k - half * kMaxRows * kWPad;
+                const int r = rem / kWPad, j = rem - r * kWPad;
+                float v = 0.0f;
+                if (r < tab.rows && j < tab.row_deg[r]) v = (half ? wcur : wprev)[tab.row_ptr[r] + j];
+                wp[k] = v;
+            }
         }
         if (tid < cpb) s_fail[tid] = 0;
         __syncthreads();
         const bool act = !slot_done;
         const bool store = !last || out.app != nullptr;
-        iterate_rows<WEIGHTED, LAYERED>(tab, s, s4old, dnew, wprev, wcur, st_base, gllr, hd_base, act, first, store,
+        iterate_rows<WEIGHTED, LAYERED>(tab, s, s4old, dnew, wpad, st_base, gllr, hd_base, act, first, store,
                                         early_stop || last, alpha);
         if (early_stop && !last) {  // the rows ended with a barrier
             if (act) check_rows(tab, s, s4old + dnew, hd_base, &s_fail[slot]);
@@ -451,7 +471,8 @@ __global__ void __launch_bounds__(kMaxThreads, MINB)
     const uint32_t bar = smem_addr(smem);
     int* s_group = reinterpret_cast<int*>(smem + 8);
     int* s_fail = reinterpret_cast<int*>(smem + 16);
-    float* buf0 = reinterpret_cast<float*>(smem + kHeaderBytes);
+    float4* wpad = reinterpret_cast<float4*>(smem + kHeaderBytes);
+    float* buf0 = reinterpret_cast<float*>(smem + kHeaderBytes + kWeightBytes);
     const float* wtab = nullptr;
     if constexpr (WEIGHTED) wtab = &wt.w[0][0];
 
@@ -497,7 +518,7 @@ __global__ void __launch_bounds__(kMaxThreads, MINB)
         SlotOut out{a.packed + cw * tab.packed_bytes, a.app ? a.app + cw * n : nullptr,
                     a.iters ? a.iters + cw : nullptr};
         run_group<WEIGHTED, LAYERED>(tab, cpb, slot, s, slot_done, buf0, hd0, s_fail, st_base, a.llr + cw * n, out,
-                                     a.n_iter, a.early_stop, a.alpha, wtab, a.n_w_iters);
+                                     a.n_iter, a.early_stop, a.alpha, wtab, wpad, a.n_w_iters);
     }
 }
 
@@ -559,14 +580,14 @@ __global__ void __launch_bounds__(kMaxThreads, 2)
         uint4* st_base = reinterpret_cast<uint4*>(a.state + static_cast<size_t>(blockIdx.x) * a.slot_words) +
                          static_cast<size_t>(valid_thread ? slot : 0) * tab.rows * z;
         run_group<false, false>(tab, cpb, slot, s, !valid_thread, buf0, hd0, s_fail, st_base,
-                         a.llr + job.llr_offset, out, a.n_iter, a.early_stop, a.alpha, nullptr, 1);
+                         a.llr + job.llr_offset, out, a.n_iter, a.early_stop, a.alpha, nullptr, nullptr, 1);
     }
 }
 
 }  // namespace
 
 size_t decode_smem_bytes(const CodeTable& tab, int cpb) {
-    return kHeaderBytes + group_smem_bytes(tab, cpb);
+    return kHeaderBytes + kWeightBytes + group_smem_bytes(tab, cpb);
 }
 
 template <bool W, int MINB, bool LAY>
