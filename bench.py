@@ -462,7 +462,7 @@ def main():
         line["learned_vs_plain"] = lvp
     line.update(extra)
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(llr.cpu().numpy(), n_sample=min(B, 1024))
+        line["cpu_baseline"] = cpu_baseline(llr.cpu().numpy(), n_sample=B)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

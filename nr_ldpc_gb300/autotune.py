@@ -1,7 +1,8 @@
 """Autotuner for codewords per CTA, per (BG, Z).
 
 The decode CTA holds `cw_per_cta` codewords of one code (threads = cw_per_cta
-* Z, at most 384; two fp32 posterior buffers per codeword in shared memory).
+* Z, at most 384; two fp32 posterior buffers over each codeword's core columns
+in shared memory, two CTAs per SM).
 Fewer codewords per CTA balance early-stopping codewords better; more keep
 the SM busier.  For each code this times the persistent batch decode of a
 homogeneous job list at every admissible value and keeps the fastest; the

@@ -191,7 +191,8 @@ int init_impl(const int* base, int rows, int cols, int kb, const nrldpc_config* 
         delete h;
         return NRLDPC_ERR_CUDA;
     }
-    // one CTA per SM by shared memory -> give it the full register budget
+    // two CTAs per SM when shared memory allows (the kernel then caps its
+    // registers for two); otherwise one CTA with the full register budget
     h->minb = (2 * (h->smem + 1024) <= prop.sharedMemPerMultiprocessor) ? 2 : 1;
     h->ctas_per_sm = std::max(1, std::min(decode_max_ctas_per_sm(false, h->minb, h->threads, h->smem),
                                           decode_max_ctas_per_sm(true, h->minb, h->threads, h->smem)));
