@@ -1,0 +1,46 @@
+"""The C++ layer (include/nr_ldpc_gb300.hpp) from a reference-style host
+program: it compiles and links against the in-tree library with plain g++
+(CPU), and its decode equals the oracle's (GPU)."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from nr_ldpc_gb300 import codes
+from oracle.oracle import OracleCode
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+
+
+def _build(tmp_path, cuda_lib):
+    exe = str(tmp_path / "host_decode")
+    cmd = ["g++", "-std=c++17", "-O2", os.path.join(ROOT, "tests", "cpp", "host_decode.cpp"), "-o", exe,
+           "-I", os.path.join(ROOT, "include"), "-I", os.path.join(CUDA, "include"),
+           "-L", os.path.join(ROOT, "nr_ldpc_gb300"), "-lnrldpc_gb300",
+           "-Wl,-rpath," + os.path.join(ROOT, "nr_ldpc_gb300"),
+           "-L", os.path.join(CUDA, "lib64"), "-lcudart", "-Wl,-rpath," + os.path.join(CUDA, "lib64")]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    return exe
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="g++ not present")
+def test_cpp_caller_compiles_and_links(tmp_path, cuda_lib):
+    assert os.path.exists(_build(tmp_path, cuda_lib))
+
+
+@pytest.mark.gpu
+def test_cpp_caller_decodes_like_the_oracle(tmp_path, cuda_lib):
+    exe = _build(tmp_path, cuda_lib)
+    oc = OracleCode(codes.base_matrix(1, codes.set_index(384)), 384)
+    sig = np.full(6, codes.noise_sigma(1.7, 1 / 3), np.float32)
+    llr, _ = oc.gen_llr(22, 5150, 0, sig, 2)
+    src, dst = tmp_path / "llr.f32", tmp_path / "out.u8"
+    llr.tofile(src)
+    r = subprocess.run([exe, "8424", "10", str(src), str(dst)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    want, _, _ = oc.minsum_f32(llr, 10)
+    got = np.fromfile(dst, np.uint8).reshape(want.shape)
+    np.testing.assert_array_equal(got, want)

@@ -142,3 +142,11 @@ def test_layered_short_training_lowers_the_loss(gpu):
     hist = tr.train(25)
     assert np.mean(hist[-5:]) < np.mean(hist[:5])
     assert np.isfinite(hist).all()
+
+
+def test_weight_rows_limit(gpu):
+    from nr_ldpc_gb300 import _lib
+    dec = Decoder(bg=2, z=16, max_batch=4)
+    with pytest.raises(_lib.NrLdpcError):
+        dec.set_weights(np.full((17, dec.n_edges), 0.75, np.float32))
+    dec.set_weights(np.full((16, dec.n_edges), 0.75, np.float32))  # the maximum is accepted
