@@ -320,6 +320,15 @@ def cpu_baseline(llr_host: np.ndarray, n_sample: int):
             "value_1thread": n1 * K_INFO / dt1 / 1e9}
 
 
+def workload_config(batch: int) -> dict:
+    """The workload both arms measure (the reference arm times a bounded
+    sample of it on the host cores)."""
+    return {"workload": "BG1 Z=384 normalized min-sum (alpha 0.75) flooding decode, "
+                        f"batch {batch}, {ITERS} iterations, early stop off",
+            "ebn0_db": EBN0, "codewords_per_gpu": batch, "info_bits": K_INFO,
+            "l2_policy": f"inputs larger than L2 ({batch * N_BP * 4 / 1e6:.0f} MB LLR batch per step)"}
+
+
 def run_reference(args, world, rank):
     """--impl reference: the reference algorithm on the host cores (oracle
     port; the reference's own decoder exists only as CUDA kernels that do not
@@ -347,8 +356,7 @@ def run_reference(args, world, rank):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded Philox info bits, BPSK/AWGN LLRs)",
-        "config": {"workload": f"BG1 Z=384 min-sum decode, {ITERS} iterations, Eb/N0 {EBN0} dB",
-                   "codewords_per_step": n_step, "threads": cores},
+        "config": dict(workload_config(BATCH), reference_sample_codewords_per_step=n_step, threads=cores),
         "cpu_baseline": {"value": value, "unit": "Gbit/s", "cores": cores, "kind": "port",
                          "sample": f"{n_step} codewords per step on {cores} threads"},
         "e2e": {"value": value, "unit": "Gbit/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -438,12 +446,8 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded Philox info bits, structural encoder, BPSK/AWGN LLRs)",
-        "config": {"workload": "BG1 Z=384 normalized min-sum (alpha 0.75) flooding decode, "
-                               f"batch {B}, {ITERS} iterations, early stop off",
-                   "ebn0_db": EBN0, "codewords_per_gpu": B, "info_bits": K_INFO,
-                   "fer": frame_err / B, "ber": bit_err / (B * K_INFO),
-                   "l2_policy": f"inputs larger than L2 ({B * N_BP * 4 / 1e6:.0f} MB LLR batch per step)",
-                   "parallelism": f"replicas x{world}"},
+        "config": dict(workload_config(B), fer=frame_err / B, ber=bit_err / (B * K_INFO),
+                       parallelism=f"replicas x{world}"),
         "cw_per_s": world * B / (ms_step * 1e-3),
         "e2e": {"value": world * B * K_INFO / (e2e_ms * 1e-3) / 1e9, "unit": "Gbit/s",
                 "h2d_bytes_per_step": B * N_BP * 4, "d2h_bytes_per_step": B * dec.packed_bytes,
