@@ -185,6 +185,10 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
         const float qa = fabsf(q);
         // sign bit of q + 0 is (q < 0): -0 becomes +0, NaN results are canonical (+)
         qmask = __funnelshift_l(__float_as_uint(__fadd_rn(q, 0.0f)), qmask, 1);  // edge i at bit D-1-i
+        if (i == 0) {  // from m1 = m2 = 1000: min2 stays 1000 whatever |Q_0| is
+            m1 = fminf(m1, qa);
+            continue;
+        }
         if (qa < m1) idx = i;
         const float mx = max_nan(m1, qa);  // NaN |Q| leaves min1/min2 untouched
         m1 = fminf(m1, qa);

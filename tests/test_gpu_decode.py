@@ -248,3 +248,20 @@ def test_host_call_in_chunks_back_to_back(gpu):
     dec.decode_host_q(q.pin_memory(), out_q, 7, stream=s)
     s.synchronize()
     assert torch.equal(out_q, dec.decode(q.to(gpu).float(), 7).cpu())
+
+
+def test_posterior_within_1e5_of_fp64_transcription(gpu):
+    """GPU posteriors against the oracle's FP64 min-sum at 1-3 iterations:
+    within 1e-5 relative (floor 1) for 99.9% of positions, hard decisions
+    differing only where an fp32 rounding flipped a min or a sign."""
+    dec = Decoder(bg=1, z=384, max_batch=4)
+    oc = oracle_for(dec)
+    sig = np.full(4, codes.noise_sigma(2.0, 1 / 3), np.float32)
+    llr, _ = oc.gen_llr(22, 71, 0, sig, 2)
+    for it in (1, 2, 3):
+        pk, app = dec.decode(torch.from_numpy(llr).to(gpu), it, want_app=True)
+        torch.cuda.synchronize()
+        p64, a64, _ = oc.minsum_f64(llr.astype(np.float64), it)
+        rel = np.abs(app.cpu().numpy() - a64) / np.maximum(np.abs(a64), 1.0)
+        assert np.quantile(rel, 0.999) < 1e-5, (it, np.quantile(rel, 0.999))
+        assert (np.unpackbits(pk.cpu().numpy() ^ p64, axis=1)).sum() <= 8
