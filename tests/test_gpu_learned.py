@@ -150,3 +150,32 @@ def test_weight_rows_limit(gpu):
     with pytest.raises(_lib.NrLdpcError):
         dec.set_weights(np.full((17, dec.n_edges), 0.75, np.float32))
     dec.set_weights(np.full((16, dec.n_edges), 0.75, np.float32))  # the maximum is accepted
+
+
+def test_trained_weights_gain_over_plain(gpu):
+    """What the trained network adds (committed weights/bg1_L6, BG1 Z=384,
+    1.8 dB, 16384 seeded codewords, early stop): the learned layered decoder
+    at <= 6 iterations has a lower FER than the same layered decoder with the
+    plain alpha = 0.75 and than plain flooding min-sum at 10 iterations."""
+    from nr_ldpc_gb300.learned import load_weights
+    n = 8192
+    dec = Decoder(bg=1, z=384, max_batch=n)
+    sig = torch.full((n,), codes.noise_sigma(1.8, 22 / 66), device=gpu)
+    sets = [dec.gen_llr(seed=404, cw_base=k * n, sigma=sig) for k in range(2)]
+
+    def fer(schedule, weights, iters):
+        dec.set_schedule(schedule)
+        if weights is not None:
+            dec.set_weights(load_weights(weights))
+        counts = torch.zeros(2, dtype=torch.int64, device=gpu)
+        for llr, cw in sets:
+            pk = dec.decode(llr, iters, early_stop=True, weighted=weights is not None)
+            dec.count_errors(pk, cw, counts=counts)
+        torch.cuda.synchronize()
+        return int(counts[1]) / (2 * n)
+
+    learned = fer("layered", "bg1_L6", 6)
+    plain_layered = fer("layered", None, 6)
+    plain_flooding = fer("flooding", None, 10)
+    assert learned < 0.2 * plain_layered and learned < 0.2 * plain_flooding, (learned, plain_layered, plain_flooding)
+    assert plain_flooding <= 1e-2  # the operating point: plain min-sum at 10 iterations has FER <= 1e-2
