@@ -13,17 +13,19 @@ from oracle.oracle import OracleCode, RefEmu
 
 
 @pytest.mark.skipif(not RefEmu.available("bg1"), reason="oracle/_ref needs the reference tree")
-def test_fer_matches_reference_channel_pipeline():
-    n, ebn0, it = 240, 1.6, 10
+@pytest.mark.parametrize("ebn0", [1.5, 1.6, 1.7])
+def test_fer_matches_reference_channel_pipeline(ebn0):
+    """One point of the FER curve per Eb/N0 in the waterfall."""
+    n, it = 240, 10
     H = codes.base_matrix(1, 1)
     oc = OracleCode(H, 384)
     ref = RefEmu(H, 384)
-    llr_r, info_r = ref.transmit_llr(8424, 1 / 3, n, ebn0, 69012, 8448, 26112)
+    llr_r, info_r = ref.transmit_llr(8424, 1 / 3, n, ebn0, 69012 + int(ebn0 * 100), 8448, 26112)
     pk, _, _ = oc.minsum_f32(llr_r, it, threads=8)
     bits = np.unpackbits(pk, axis=1, bitorder="little")[:, :8448]
     fe_ref = int((bits != info_r).any(axis=1).sum())
     sig = np.full(n, codes.noise_sigma(ebn0, 1 / 3), np.float32)
-    llr_o, cw = oc.gen_llr(22, 777, 0, sig, 2)
+    llr_o, cw = oc.gen_llr(22, 777 + int(ebn0 * 100), 0, sig, 2)
     pk, _, _ = oc.minsum_f32(llr_o, it, threads=8)
     fe_own = int((np.unpackbits(pk ^ cw, axis=1, bitorder="little")[:, :8448]).any(axis=1).sum())
     lo_r, hi_r = clopper_pearson(fe_ref, n)

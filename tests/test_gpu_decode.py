@@ -265,3 +265,31 @@ def test_posterior_within_1e5_of_fp64_transcription(gpu):
         rel = np.abs(app.cpu().numpy() - a64) / np.maximum(np.abs(a64), 1.0)
         assert np.quantile(rel, 0.999) < 1e-5, (it, np.quantile(rel, 0.999))
         assert (np.unpackbits(pk.cpu().numpy() ^ p64, axis=1)).sum() <= 8
+
+
+ALL_Z = sorted({a << j for a in (2, 3, 5, 7, 9, 11, 13, 15) for j in range(8) if a << j <= 384})
+
+
+@pytest.mark.parametrize("bg", [1, 2])
+def test_every_lifting_size_against_oracle(gpu, bg):
+    """All 51 lifting sizes of the base graph (every shift table, Z from 2 to
+    384, cw_per_cta from 1 to 48): flooding with early stop and layered
+    decodes of seeded codewords equal the oracle bit for bit."""
+    for z in ALL_Z:
+        n = 3
+        dec = Decoder(bg=bg, z=z, max_batch=n)
+        oc = oracle_for(dec)
+        rate = dec.kb / (dec.cols - 2)
+        sig = np.linspace(codes.noise_sigma(1.2, rate), codes.noise_sigma(2.2, rate), n).astype(np.float32)
+        llr, _ = oc.gen_llr(dec.kb, 500 + z, 0, sig, 2)
+        d_llr = torch.from_numpy(llr).to(gpu)
+        pk, it = dec.decode(d_llr, 4, early_stop=True, want_iters=True)
+        dec.set_schedule("layered")
+        pl = dec.decode(d_llr, 3)
+        torch.cuda.synchronize()
+        opk, _, oit = oc.minsum_f32(llr, 4, early_stop=True, threads=3)
+        np.testing.assert_array_equal(pk.cpu().numpy(), opk, err_msg=f"flooding bg{bg} z{z}")
+        np.testing.assert_array_equal(it.cpu().numpy(), oit, err_msg=f"iterations bg{bg} z{z}")
+        opl, _, _ = oc.layered_f32(llr, 3, threads=3)
+        np.testing.assert_array_equal(pl.cpu().numpy(), opl, err_msg=f"layered bg{bg} z{z}")
+        dec.close()
