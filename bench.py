@@ -14,7 +14,10 @@ min-sum at a stated Eb/N0 where plain flooding at 10 iterations has FER <=
 1e-2: FER with 95% intervals over 65,536 fresh codewords and info Gbit/s of
 each (early stop on for both).  ``mixed_batch`` times the uneven (BG, Z,
 rate-matched) 8192-codeword workload in one launch; ``training`` the learned
-decoder's training step (BG2 Z=128, 8 iterations, 16384 codewords).
+decoder's training step (BG2 Z=128, 8 iterations, 16384 codewords);
+``c1_fer_curve`` the FER curve of the bench code over Eb/N0 0.5-2.5 dB;
+``c0_default_code`` the reference README's workload (640 codewords of its
+default 12x24 rate-1/2 code, 5 iterations, SNR 0-10 dB).
 
 Under torchrun each rank decodes its own batch (codewords are independent:
 replicas, weak scaling); rank 0 prints one JSON line with the max time over
@@ -298,6 +301,65 @@ def training_step(steps: int = 5):
             "codewords_per_s": 16384 / (ms * 1e-3), "steps_timed": steps}
 
 
+def c1_fer_curve(dec, batch: int = 4096):
+    """BG1 Z=384 plain min-sum at 10 iterations over Eb/N0 0.5-2.5 dB (step
+    0.25), one fresh 4096-codeword batch per point: BER, FER with 95%
+    Clopper-Pearson interval, early stop off; and the average iterations with
+    early stop on."""
+    import torch
+    from nr_ldpc_gb300 import codes
+    from nr_ldpc_gb300.evaluate import clopper_pearson
+    out = torch.empty((batch, dec.packed_bytes), dtype=torch.uint8, device="cuda")
+    pts = []
+    for k in range(9):
+        eb = 0.5 + 0.25 * k
+        sig = torch.full((batch,), codes.noise_sigma(eb, K_INFO / (N_BP - 2 * Z)), device="cuda")
+        llr, cw = dec.gen_llr(seed=61, cw_base=k * batch, sigma=sig)
+        counts = dec.count_errors(dec.decode(llr, ITERS, out=out), cw)
+        _, its = dec.decode(llr, ITERS, early_stop=True, want_iters=True, out=out)
+        be, fe = (int(x) for x in counts.tolist())
+        lo, hi = clopper_pearson(fe, batch)
+        pts.append({"ebn0_db": eb, "ber": be / (batch * K_INFO), "fer": fe / batch, "fer_ci95": [lo, hi],
+                    "avg_iters_early_stop": float(its.float().mean().item())})
+    return {"code": "BG1 Z=384", "iterations": ITERS, "codewords_per_point": batch, "points": pts}
+
+
+def c0_default_code(n: int = 640, n_iter: int = 5, reps: int = 20):
+    """The reference's README workload on its default 12x24 rate-1/2 code
+    (stand-in: the 802.11n matrix of its Overview, lifted at Z=96; N=2304,
+    K=1152): 640 codewords per SNR point 0-10 dB, 5 iterations.  BER/FER per
+    point, and the batch decode time through the host-buffer call (copies
+    included, as the README's timings are)."""
+    import torch
+    from nr_ldpc_gb300 import Decoder, codes
+    dec = Decoder(z=96, base=codes.wifi_base(), max_batch=n)
+    k_info = dec.kb * dec.z
+    pts = []
+    for snr in range(11):
+        sig = torch.full((n,), codes.noise_sigma(float(snr), 0.5), device="cuda")
+        llr, cw = dec.gen_llr(seed=71, cw_base=snr * n, sigma=sig, n_punct_cols=0)
+        counts = dec.count_errors(dec.decode(llr, n_iter), cw)
+        be, fe = (int(x) for x in counts.tolist())
+        pts.append({"snr_db": snr, "ber": be / (n * k_info), "fer": fe / n})
+    llr_h = llr.cpu().pin_memory()
+    out_h = torch.empty((n, dec.packed_bytes), dtype=torch.uint8).pin_memory()
+    stream = torch.cuda.Stream()
+    for _ in range(3):
+        dec.decode_host(llr_h, out_h, n_iter, stream=stream)
+    stream.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        dec.decode_host(llr_h, out_h, n_iter, stream=stream)
+        stream.synchronize()
+    ms = 1e3 * (time.perf_counter() - t0) / reps
+    dec.close()
+    return {"code": "12x24 rate-1/2 stand-in (802.11n matrix, Z=96): N=2304, K=1152", "iterations": n_iter,
+            "codewords": n, "ms_per_batch_host_buffers": ms, "cw_per_s": n / (ms * 1e-3),
+            "info_mbps": n * k_info / (ms * 1e-3) / 1e6, "points": pts,
+            "reference_readme": "16.83-16.99 ms per 640 codewords, 43.4-43.8 Mbit/s info "
+                                "(GeForce GTX 950M, its original 12x24 code)"}
+
+
 def cpu_baseline(llr_host: np.ndarray, n_sample: int):
     """Reference algorithm on the host cores: the oracle's C restatement of
     the reference min-sum (kind 'port'), all cores, one codeword per thread."""
@@ -434,8 +496,15 @@ def main():
         e2e_ms = run_e2e(dec, llr, packed, args.steps, stream, world)
 
     lvp, lvp_launches = (None, 0) if args.no_learned else learned_vs_plain(dec, stream, min(B, 4096))
-    extra = {} if args.no_extra or rank != 0 else {"mixed_batch": mixed_batch(stream),
-                                                    "training": training_step()}
+    extra = {}
+    if not args.no_extra and rank == 0:
+        for name, leg in (("mixed_batch", lambda: mixed_batch(stream)), ("training", training_step),
+                          ("c1_fer_curve", lambda: c1_fer_curve(dec, min(B, 4096))),
+                          ("c0_default_code", c0_default_code)):
+            try:  # a failing side measurement must not cost the headline line
+                extra[name] = leg()
+            except Exception as exc:  # noqa: BLE001
+                extra[name] = {"error": f"{type(exc).__name__}: {exc}"}
 
     peak, peak_kind = measured_peaks()
     bytes_launch = model_bytes_per_cw(ITERS) * B
