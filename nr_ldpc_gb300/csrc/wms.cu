@@ -178,13 +178,18 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
             const uint4* st_prev =
                 a.states + static_cast<size_t>(t > 0 ? t - 1 : 0) * a.n_cw * rows * z + cw_off;
             uint4* st_cur = a.states + static_cast<size_t>(t) * a.n_cw * rows * z + cw_off;
+            // previous iteration's state of row r+2 requested while row r runs
+            auto fetch = [&](int r) -> uint4 {
+                return (act && t > 0 && r < rows) ? __ldcg(st_prev + r * z + s) : make_uint4(0u, 0u, 0u, 0u);
+            };
+            uint4 p0 = fetch(0), p1 = fetch(1);
             for (int r = 0; r < rows; r++) {
-                if (act) {
-                    uint4 st = make_uint4(0u, 0u, 0u, 0u);
-                    if (t > 0) st = __ldcg(st_prev + r * z + s);
+                const uint4 p2 = fetch(r + 2);
+                if (act)
                     fwd_dispatch<LAYERED>(tab.row_deg[r], tab, tab.row_ptr[r], s, lold, lnew, wbuf,
-                                 wbuf + kMaxEdges, st, st_cur + r * z + s);
-                }
+                                          wbuf + kMaxEdges, p0, st_cur + r * z + s);
+                p0 = p1;
+                p1 = p2;
                 if (tab.sync_after[r]) __syncthreads();
             }
             // loss term and its gradient seed at L^{t+1}
@@ -221,13 +226,12 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
 template <int D>
 __device__ __forceinline__ void bwd_row(const CodeTable& tab, int e0, uint32_t s, bool act,
                                         const float* gl, float* gl_next, const float* w_cur,
-                                        float* gw_acc, uint4 st, uint4* gq_io, bool scatter) {
+                                        float* gw_acc, uint4 st, uint4 gin, uint4* gq_io, bool scatter) {
     const uint32_t z = static_cast<uint32_t>(tab.z);
     const float m1 = __uint_as_float(st.x), m2 = __uint_as_float(st.y);
     const int i1 = static_cast<int>(st.z & 31u), i2 = static_cast<int>(st.w);
     const uint32_t q = st.z >> 8;
     const uint32_t par = static_cast<uint32_t>(__popc(q) & 1);
-    uint4 gin = act ? *gq_io : make_uint4(0u, 0u, 31u, 31u);
     const float g1n = __uint_as_float(gin.x), g2n = __uint_as_float(gin.y);
     const int j1 = static_cast<int>(gin.z), j2 = static_cast<int>(gin.w);
     uint32_t ad1 = 0, ad2 = 0;  // columns of the two argmin edges
@@ -265,10 +269,10 @@ __device__ __forceinline__ void bwd_row(const CodeTable& tab, int e0, uint32_t s
 
 __device__ __forceinline__ void bwd_dispatch(int deg, const CodeTable& tab, int e0, uint32_t s,
                                              bool act, const float* gl, float* gln, const float* wc,
-                                             float* gw_acc, uint4 st, uint4* gq, bool scatter) {
+                                             float* gw_acc, uint4 st, uint4 gin, uint4* gq, bool scatter) {
     switch (deg) {
 #define NRLDPC_BWD_CASE(D) \
-    case D: bwd_row<D>(tab, e0, s, act, gl, gln, wc, gw_acc, st, gq, scatter); break;
+    case D: bwd_row<D>(tab, e0, s, act, gl, gln, wc, gw_acc, st, gin, gq, scatter); break;
         NRLDPC_BWD_CASE(1) NRLDPC_BWD_CASE(2) NRLDPC_BWD_CASE(3) NRLDPC_BWD_CASE(4)
         NRLDPC_BWD_CASE(5) NRLDPC_BWD_CASE(6) NRLDPC_BWD_CASE(7) NRLDPC_BWD_CASE(8)
         NRLDPC_BWD_CASE(9) NRLDPC_BWD_CASE(10) NRLDPC_BWD_CASE(11) NRLDPC_BWD_CASE(12)
@@ -318,10 +322,27 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
             }
             __syncthreads();
             const uint4* st = a.states + (static_cast<size_t>(t) * a.n_cw + (act ? cw : 0)) * rows * z;
+            // state and per-row dloss/dQ of row r+2 requested while row r runs
+            auto fetch = [&](int r, uint4& sv, uint4& gv) {
+                sv = make_uint4(0u, 0u, 0u, 31u);
+                gv = make_uint4(0u, 0u, 31u, 31u);
+                if (act && r < rows) {
+                    sv = __ldcg(st + r * z + s);
+                    gv = __ldcg(gq + r * z + s);
+                }
+            };
+            uint4 s0, g0, s1, g1;
+            fetch(0, s0, g0);
+            fetch(1, s1, g1);
             for (int r = 0; r < rows; r++) {
-                const uint4 sv = act ? __ldcg(st + r * z + s) : make_uint4(0u, 0u, 0u, 31u);
-                bwd_dispatch(tab.row_deg[r], tab, tab.row_ptr[r], s, act, gl, gln, wcur, gw_acc, sv,
+                uint4 s2, g2;
+                fetch(r + 2, s2, g2);
+                bwd_dispatch(tab.row_deg[r], tab, tab.row_ptr[r], s, act, gl, gln, wcur, gw_acc, s0, g0,
                              gq + r * z + s, t > 0);
+                s0 = s1;
+                g0 = g1;
+                s1 = s2;
+                g1 = g2;
             }
             __syncthreads();
             for (int e = tid; e < E; e += blockDim.x)
@@ -429,10 +450,16 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
             }
             __syncthreads();
             const uint4* st = a.states + (static_cast<size_t>(t) * a.n_cw + (act ? cw : 0)) * rows * z;
+            auto fetch = [&](int r) -> uint4 {  // state of row r-2 requested while row r runs
+                return (act && r >= 0) ? __ldcg(st + r * z + s) : make_uint4(0u, 0u, 0u, 31u);
+            };
+            uint4 s0 = fetch(rows - 1), s1 = fetch(rows - 2);
             for (int r = rows - 1; r >= 0; r--) {
-                const uint4 sv = act ? __ldcg(st + r * z + s) : make_uint4(0u, 0u, 0u, 31u);
-                bwd_layered_dispatch(tab.row_deg[r], tab, tab.row_ptr[r], s, act, g, wcur, gw_acc, sv,
+                const uint4 s2 = fetch(r - 2);
+                bwd_layered_dispatch(tab.row_deg[r], tab, tab.row_ptr[r], s, act, g, wcur, gw_acc, s0,
                                      gh + static_cast<size_t>(tab.row_ptr[r]) * z + s, t < a.T - 1, t > 0);
+                s0 = s1;
+                s1 = s2;
                 if (r > 0 && tab.sync_after[r - 1]) __syncthreads();
             }
             __syncthreads();
