@@ -222,6 +222,41 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
     }
 }
 
+// Sums v[i] over the 32 lanes of the warp for every i < D and adds the sums
+// to acc[i] (shared memory), one atomic per edge: a transposing butterfly
+// (at each level a lane keeps one half of its values and trades the other
+// half with its partner, P - 1 shuffles for P = D rounded up to a power of
+// two) followed by a plain reduction over the remaining lane bits, instead of
+// a 5-shuffle reduction per value.
+template <int D>
+__device__ __forceinline__ void warp_sum_to(float (&v)[D], float* acc) {
+    constexpr int P = D <= 1 ? 1 : D <= 2 ? 2 : D <= 4 ? 4 : D <= 8 ? 8 : D <= 16 ? 16 : 32;
+    constexpr int LOGP = P == 1 ? 0 : P == 2 ? 1 : P == 4 ? 2 : P == 8 ? 3 : P == 16 ? 4 : 5;
+    const int lane = static_cast<int>(threadIdx.x & 31u);
+    float w[P];
+#pragma unroll
+    for (int j = 0; j < P; j++) w[j] = j < D ? v[j] : 0.0f;
+#pragma unroll
+    for (int lvl = 0; lvl < LOGP; lvl++) {
+        const int k = P >> (lvl + 1);  // values kept after this level
+        const int o = 16 >> lvl;       // partner lane distance
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int j = 0; j < k; j++) {
+            const float send = up ? w[j] : w[j + k];
+            const float keep = up ? w[j + k] : w[j];
+            w[j] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+    }
+#pragma unroll
+    for (int o = 16 >> LOGP; o > 0; o >>= 1) w[0] += __shfl_xor_sync(0xffffffffu, w[0], o);
+    // lane L now holds the sum for value L >> (5 - LOGP)
+    if ((lane & ((32 >> LOGP) - 1)) == 0) {
+        const int i = lane >> (5 - LOGP);
+        if (i < D) atomicAdd(&acc[i], w[0]);
+    }
+}
+
 // ---- adjoint ------------------------------------------------------------------------
 template <int D>
 __device__ __forceinline__ void bwd_row(const CodeTable& tab, int e0, uint32_t s, bool act,
@@ -236,6 +271,7 @@ __device__ __forceinline__ void bwd_row(const CodeTable& tab, int e0, uint32_t s
     const int j1 = static_cast<int>(gin.z), j2 = static_cast<int>(gin.w);
     uint32_t ad1 = 0, ad2 = 0;  // columns of the two argmin edges
     float acc1 = 0.0f, acc2 = 0.0f;
+    float gwv[D];
 #pragma unroll
     for (int i = 0; i < D; i++) {
         const uint32_t ed = tab.edge[e0 + i];
@@ -247,13 +283,12 @@ __device__ __forceinline__ void bwd_row(const CodeTable& tab, int e0, uint32_t s
         if (act) gr = gl[a] - (i == j1 ? g1n : (i == j2 ? g2n : 0.0f));
         const float sg = ((par ^ (q >> i)) & 1u) ? -1.0f : 1.0f;
         const float mag = i == i1 ? m2 : m1;
-        float gw = act ? gr * sg * mag : 0.0f;
-        for (int off = 16; off > 0; off >>= 1) gw += __shfl_xor_sync(0xffffffffu, gw, off);
-        if ((threadIdx.x & 31) == 0) atomicAdd(&gw_acc[e0 + i], gw);
+        gwv[i] = act ? gr * sg * mag : 0.0f;
         const float t = gr * w_cur[e0 + i] * sg;
         if (i == i1) acc2 = t;
         else acc1 += t;
     }
+    warp_sum_to<D>(gwv, gw_acc + e0);
     float g1 = 0.0f, g2 = 0.0f;
     if (act) {
         if (m1 < 1000.0f) g1 = acc1 * (((q >> i1) & 1u) ? -1.0f : 1.0f);
@@ -366,6 +401,7 @@ __device__ __forceinline__ void bwd_layered_row(const CodeTable& tab, int e0, ui
     const uint32_t par = static_cast<uint32_t>(__popc(q) & 1);
     uint32_t ad[D];
     float ga[D];
+    float gwv[D];
     float to1 = 0.0f, to2 = 0.0f;  // dloss/dQ at the argmin edges through R
 #pragma unroll
     for (int i = 0; i < D; i++) {
@@ -381,13 +417,12 @@ __device__ __forceinline__ void bwd_layered_row(const CodeTable& tab, int e0, ui
         }
         const float sg = ((par ^ (q >> i)) & 1u) ? -1.0f : 1.0f;
         const float mag = i == i1 ? m2 : m1;
-        float gw = act ? dr * sg * mag : 0.0f;
-        for (int off = 16; off > 0; off >>= 1) gw += __shfl_xor_sync(0xffffffffu, gw, off);
-        if ((threadIdx.x & 31) == 0) atomicAdd(&gw_acc[e0 + i], gw);
+        gwv[i] = act ? dr * sg * mag : 0.0f;
         const float t = dr * w_cur[e0 + i] * sg;
         if (i == i1) to2 = t;
         else to1 += t;
     }
+    warp_sum_to<D>(gwv, gw_acc + e0);
     if (!act) return;
     const float g1 = m1 < 1000.0f ? to1 * (((q >> i1) & 1u) ? -1.0f : 1.0f) : 0.0f;
     const float g2 = (i2 < D && m2 < 1000.0f) ? to2 * (((q >> i2) & 1u) ? -1.0f : 1.0f) : 0.0f;
