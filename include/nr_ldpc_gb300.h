@@ -105,7 +105,10 @@ int nrldpc_decode(nrldpc_handle* h, const float* d_llr, uint8_t* d_packed, int n
                   int early_stop, float* d_app, int32_t* d_iters, nrldpc_stream_t stream);
 
 /* Host buffers (pinned for overlap, pageable works): H2D into the handle's
- * staging, decode, D2H -- queued on `stream`, returns without waiting. */
+ * staging, decode, D2H -- queued on `stream`, returns without waiting.  The
+ * batch moves in chunks: the host->device copy of chunk k+1 runs on the
+ * handle's own copy stream while chunk k decodes on `stream`; all of it is
+ * ordered after earlier work on `stream` and done when `stream` is. */
 int nrldpc_decode_host_async(nrldpc_handle* h, const float* h_llr, uint8_t* h_packed, int n_cw,
                              int n_iter, int early_stop, nrldpc_stream_t stream);
 
