@@ -10,8 +10,11 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <memory>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
+#include <vector>
 
 #include "nr_ldpc_gb300.h"
 
@@ -57,6 +60,15 @@ public:
               "perform_gpu_ldpc_decoding");
     }
 
+    // The reference's char / half builds (CHAR_PRC / HALF_PRC): narrow LLRs over
+    // the host link, qtype 1 = fp16, 2 = int8 with LLR = q * scale.
+    void perform_gpu_ldpc_decoding_q(const void* h_llr_q, int qtype, float scale, uint8_t* h_packed,
+                                     int n_cw, int n_iterations, cudaStream_t stream, bool early_stop = false) {
+        check(nrldpc_decode_host_async_q(h_, h_llr_q, qtype, scale, h_packed, n_cw, n_iterations,
+                                         early_stop ? 1 : 0, reinterpret_cast<nrldpc_stream_t>(stream)),
+              "perform_gpu_ldpc_decoding");
+    }
+
     // Device-resident variant (no copies).
     void decode(const float* d_llr, uint8_t* d_packed, int n_cw, int n_iterations,
                 cudaStream_t stream, bool early_stop = false) {
@@ -70,4 +82,60 @@ private:
     int n_bp_ = 0, packed_bytes_ = 0;
 };
 
+// ---- the reference's own call shape -------------------------------------------------
+// For a caller that keeps its structs: the same arguments as the reference's
+//   template <typename T> void perform_gpu_ldpc_decoding(dev_mem<T>* d, host_mem<T>* h,
+//       const cuda_grid* g, int n_iterations, int stream_index)   (src/gpu_decoder_top.h:13-18)
+// reading the members that call reads: h->llr_cuda[s] and h->mem_size_llr_cuda
+// (pinned LLRs of the stream's batch), h->hd_packed_cuda[s] (pinned packed
+// output), d->streams[s].  `g` is not needed (the decoder sizes its own
+// launch).  compat::setup replaces the reference's setup_dev_memory +
+// setup_gpu_grid + put_h_compact_and_params_in_constant_memory: one decoder
+// per stream, since the reference keeps one process-wide code.
+namespace compat {
+
+inline std::vector<std::unique_ptr<Decoder>>& decoders() {
+    static std::vector<std::unique_ptr<Decoder>> d;
+    return d;
+}
+inline float& char_llr_scale() {  // LLR = q * scale for the char (CHAR_PRC) build
+    static float scale = 1.0f;
+    return scale;
+}
+
+inline void setup(const nrldpc_ldpc_params& p, int n_streams, int max_cw_per_stream, float alpha = 0.75f,
+                  int device = 0) {
+    auto& d = decoders();
+    d.clear();
+    for (int s = 0; s < n_streams; s++) d.emplace_back(new Decoder(p, max_cw_per_stream, alpha, device));
+}
+
+namespace detail {
+inline void run(Decoder& dec, const float* llr, char* out, int n_cw, int it, cudaStream_t st) {
+    dec.perform_gpu_ldpc_decoding(llr, reinterpret_cast<uint8_t*>(out), n_cw, it, st);
+}
+template <typename T>
+typename std::enable_if<sizeof(T) == 1>::type run(Decoder& dec, const T* llr, char* out, int n_cw, int it,
+                                                  cudaStream_t st) {
+    dec.perform_gpu_ldpc_decoding_q(llr, 2, char_llr_scale(), reinterpret_cast<uint8_t*>(out), n_cw, it, st);
+}
+template <typename T>
+typename std::enable_if<sizeof(T) == 2>::type run(Decoder& dec, const T* llr, char* out, int n_cw, int it,
+                                                  cudaStream_t st) {
+    dec.perform_gpu_ldpc_decoding_q(llr, 1, 1.0f, reinterpret_cast<uint8_t*>(out), n_cw, it, st);
+}
+}  // namespace detail
+
+template <typename DevMem, typename HostMem, typename Grid>
+void perform_gpu_ldpc_decoding(DevMem* d, HostMem* h, const Grid* /*g*/, int n_iterations, int stream_index) {
+    auto& decs = decoders();
+    if (stream_index < 0 || stream_index >= static_cast<int>(decs.size()))
+        throw std::runtime_error("perform_gpu_ldpc_decoding: no decoder for this stream (compat::setup)");
+    Decoder& dec = *decs[stream_index];
+    const auto* llr = h->llr_cuda[stream_index];
+    const int n_cw = static_cast<int>(h->mem_size_llr_cuda / (static_cast<long>(dec.n_bp()) * sizeof(*llr)));
+    detail::run(dec, llr, h->hd_packed_cuda[stream_index], n_cw, n_iterations, d->streams[stream_index]);
+}
+
+}  // namespace compat
 }  // namespace nrldpc

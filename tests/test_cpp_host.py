@@ -15,9 +15,9 @@ ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
 
-def _build(tmp_path, cuda_lib):
-    exe = str(tmp_path / "host_decode")
-    cmd = ["g++", "-std=c++17", "-O2", os.path.join(ROOT, "tests", "cpp", "host_decode.cpp"), "-o", exe,
+def _build(tmp_path, cuda_lib, name="host_decode", std="c++17"):
+    exe = str(tmp_path / name)
+    cmd = ["g++", f"-std={std}", "-O2", os.path.join(ROOT, "tests", "cpp", name + ".cpp"), "-o", exe,
            "-I", os.path.join(ROOT, "include"), "-I", os.path.join(CUDA, "include"),
            "-L", os.path.join(ROOT, "nr_ldpc_gb300"), "-lnrldpc_gb300",
            "-Wl,-rpath," + os.path.join(ROOT, "nr_ldpc_gb300"),
@@ -29,6 +29,8 @@ def _build(tmp_path, cuda_lib):
 @pytest.mark.skipif(shutil.which("g++") is None, reason="g++ not present")
 def test_cpp_caller_compiles_and_links(tmp_path, cuda_lib):
     assert os.path.exists(_build(tmp_path, cuda_lib))
+    # the reference builds as C++14: the compat layer of the header compiles there
+    assert os.path.exists(_build(tmp_path, cuda_lib, "compat_decode", "c++14"))
 
 
 @pytest.mark.gpu
@@ -44,3 +46,20 @@ def test_cpp_caller_decodes_like_the_oracle(tmp_path, cuda_lib):
     want, _, _ = oc.minsum_f32(llr, 10)
     got = np.fromfile(dst, np.uint8).reshape(want.shape)
     np.testing.assert_array_equal(got, want)
+
+
+@pytest.mark.gpu
+def test_reference_call_shape_decodes_like_the_oracle(tmp_path, cuda_lib):
+    """perform_gpu_ldpc_decoding with the reference's arguments (structs with
+    its member names, a grid, the stream index) through nrldpc::compat, two
+    streams."""
+    exe = _build(tmp_path, cuda_lib, "compat_decode", "c++14")
+    oc = OracleCode(codes.base_matrix(1, codes.set_index(384)), 384)
+    sig = np.full(5, codes.noise_sigma(1.7, 1 / 3), np.float32)
+    llr, _ = oc.gen_llr(22, 5151, 0, sig, 2)
+    src, dst = tmp_path / "llr.f32", tmp_path / "out.u8"
+    llr.tofile(src)
+    r = subprocess.run([exe, str(src), str(dst)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    want, _, _ = oc.minsum_f32(llr, 10)
+    np.testing.assert_array_equal(np.fromfile(dst, np.uint8).reshape(want.shape), want)
