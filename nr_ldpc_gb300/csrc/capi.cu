@@ -251,7 +251,7 @@ int decode_impl(Handle* h, const float* llr, uint8_t* packed, int n_cw, int n_it
 
 // Host-buffer decode (fp32 LLRs, or narrow ones widened on the GPU: qtype 1
 // fp16, 2 int8 * scale).  The batch is cut into chunks of whole CTA rounds
-// (1, 2, then 4 rounds of max_grid * cpb codewords): chunk k+1's host->device
+// (1, 2, 4, ... rounds of max_grid * cpb codewords): chunk k+1's host->device
 // copy runs on the handle's copy stream while chunk k decodes on the caller's
 // stream, and each chunk's packed bits go back as soon as it is decoded.
 int host_decode(Handle* h, const void* h_llr, int qtype, float scale, uint8_t* h_packed, int n_cw, int n_iter,
@@ -269,7 +269,7 @@ int host_decode(Handle* h, const void* h_llr, int qtype, float scale, uint8_t* h
     for (int k = 0; begin < static_cast<size_t>(n_cw); k++) {
         size_t count = std::min(static_cast<size_t>(n_cw) - begin, rounds * round);
         if (k == kHostChunks - 1) count = static_cast<size_t>(n_cw) - begin;  // last event: the rest
-        rounds = std::min<size_t>(rounds * 2, 4);
+        rounds *= 2;  // each copy hides behind the decode of a chunk half its size
         const char* src = static_cast<const char*>(h_llr) + begin * n_bp * in_elem;
         char* dst = static_cast<char*>(stage_in) + begin * n_bp * in_elem;
         if (cudaMemcpyAsync(dst, src, count * n_bp * in_elem, cudaMemcpyHostToDevice, h->copy_stream) !=
