@@ -144,10 +144,14 @@ def barrier(world: int):
         dist.barrier()
 
 
-def run_e2e(dec, llr, packed, steps, stream, world):
+def run_e2e(dec, llr, packed, steps, stream, world, mode="auto"):
     """Same decode through the host-buffer C-ABI call: pinned host LLRs ->
-    H2D -> decode -> D2H of packed bits, each step synchronized."""
+    device -> packed bits back in host memory, each step synchronized.
+    mode: the call's host transfer ('auto' = what a caller gets by default;
+    'direct' = the kernel reads the LLRs and writes the bits over the host
+    link; 'copy' = staged chunk copies)."""
     import torch
+    dec.set_host_transfer(mode)
     b = llr.shape[0]
     llr_h = torch.empty((b, N_BP), dtype=torch.float32, pin_memory=True)
     llr_h.copy_(llr)
@@ -163,6 +167,7 @@ def run_e2e(dec, llr, packed, steps, stream, world):
     e2e_ms = 1e3 * (time.perf_counter() - t0) / steps
     e2e_ms = max_over_ranks(e2e_ms, world)
     assert torch.equal(out_h, packed.cpu()), "host-path output differs from device path"
+    dec.set_host_transfer("auto")
     return e2e_ms
 
 
@@ -492,8 +497,15 @@ def main():
 
     # ---- end to end through the host-buffer C-ABI call -----------------------------
     e2e_ms = float("nan")
+    e2e_modes = {}
     if not args.no_e2e:
         e2e_ms = run_e2e(dec, llr, packed, args.steps, stream, world)
+        for mode in ("direct", "copy"):
+            try:
+                e2e_modes[mode] = world * B * K_INFO / (run_e2e(dec, llr, packed, args.steps, stream, world,
+                                                                mode) * 1e-3) / 1e9
+            except Exception as exc:  # noqa: BLE001
+                e2e_modes[mode] = f"{type(exc).__name__}: {exc}"
 
     lvp, lvp_launches = (None, 0) if args.no_learned else learned_vs_plain(dec, stream, min(B, 4096))
     extra = {}
@@ -520,7 +532,8 @@ def main():
         "cw_per_s": world * B / (ms_step * 1e-3),
         "e2e": {"value": world * B * K_INFO / (e2e_ms * 1e-3) / 1e9, "unit": "Gbit/s",
                 "h2d_bytes_per_step": B * N_BP * 4, "d2h_bytes_per_step": B * dec.packed_bytes,
-                "ms_per_step": e2e_ms},
+                "ms_per_step": e2e_ms, "transfer": "auto",
+                "by_transfer_gbps": e2e_modes},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "traffic": None if tpc is None else tpc * B,

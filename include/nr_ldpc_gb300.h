@@ -108,7 +108,9 @@ int nrldpc_decode(nrldpc_handle* h, const float* d_llr, uint8_t* d_packed, int n
  * staging, decode, D2H -- queued on `stream`, returns without waiting.  The
  * batch moves in chunks: the host->device copy of chunk k+1 runs on the
  * handle's own copy stream while chunk k decodes on `stream`; all of it is
- * ordered after earlier work on `stream` and done when `stream` is. */
+ * ordered after earlier work on `stream` and done when `stream` is.  Pinned
+ * buffers may instead be read and written by the decoder itself over the
+ * host link (nrldpc_set_host_transfer, below). */
 int nrldpc_decode_host_async(nrldpc_handle* h, const float* h_llr, uint8_t* h_packed, int n_cw,
                              int n_iter, int early_stop, nrldpc_stream_t stream);
 
@@ -120,6 +122,21 @@ int nrldpc_decode_host_async(nrldpc_handle* h, const float* h_llr, uint8_t* h_pa
 int nrldpc_decode_host_async_q(nrldpc_handle* h, const void* h_llr_q, int qtype, float scale,
                                uint8_t* h_packed, int n_cw, int n_iter, int early_stop,
                                nrldpc_stream_t stream);
+
+/* How nrldpc_decode_host_async moves fp32 LLRs and packed bits (no reference
+ * counterpart; results are the same either way).
+ *   HOST_COPY    staged copies in chunks (the pipeline described above).
+ *   HOST_DIRECT  one launch whose threads read the LLRs from host memory and
+ *                write the packed bits back over the host link; both buffers
+ *                must be pinned (cudaHostAlloc / cudaHostRegister), else the
+ *                call returns NRLDPC_ERR_INVALID_ARG.
+ *   HOST_AUTO    (default) DIRECT when both buffers are pinned, the GPU
+ *                reaches host memory over a coherent link (Grace CPU with
+ *                NVLink-C2C: cudaDevAttrPageableMemoryAccessUsesHostPageTables)
+ *                and the batch is at most 16 rounds of the decoder's resident
+ *                CTAs (4864 BG1 Z=384 codewords on a GB300); otherwise COPY. */
+enum { NRLDPC_HOST_AUTO = 0, NRLDPC_HOST_COPY = 1, NRLDPC_HOST_DIRECT = 2 };
+int nrldpc_set_host_transfer(nrldpc_handle* h, int mode);
 
 /* Learned weighted min-sum: per (iteration, base edge) scale factors
  * w[n_w_iters][n_edges] replacing alpha (iterations past n_w_iters reuse the

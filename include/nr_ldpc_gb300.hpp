@@ -69,6 +69,10 @@ public:
               "perform_gpu_ldpc_decoding");
     }
 
+    // NRLDPC_HOST_AUTO (default), NRLDPC_HOST_COPY or NRLDPC_HOST_DIRECT: how
+    // perform_gpu_ldpc_decoding moves fp32 LLRs and bits (same results).
+    void set_host_transfer(int mode) { check(nrldpc_set_host_transfer(h_, mode), "set_host_transfer"); }
+
     // Device-resident variant (no copies).
     void decode(const float* d_llr, uint8_t* d_packed, int n_cw, int n_iterations,
                 cudaStream_t stream, bool early_stop = false) {

@@ -54,6 +54,7 @@ SIGNATURES = {
     "nrldpc_decode_host_async": (_i, [_vp, _vp, _vp, _i, _i, _i, _vp]),
     "nrldpc_decode_host_async_q": (_i, [_vp, _vp, _i, _f, _vp, _i, _i, _i, _vp]),
     "nrldpc_set_schedule": (_i, [_vp, _i]),
+    "nrldpc_set_host_transfer": (_i, [_vp, _i]),
     "nrldpc_set_weights": (_i, [_vp, _vp, _i]),
     "nrldpc_decode_weighted": (_i, [_vp, _vp, _vp, _i, _i, _i, _vp, _vp, _vp]),
     "nrldpc_wms_workspace_bytes": (_i, [_vp, _i, _i, C.POINTER(C.c_size_t)]),

@@ -20,6 +20,10 @@ namespace {
 
 const int kBaseZ[8] = {2, 3, 5, 7, 9, 11, 13, 15};
 constexpr int kHostChunks = 16;  // most chunks of one host-buffer decode
+// Largest batch, in CTA rounds, that NRLDPC_HOST_AUTO decodes straight from
+// host memory (GB300, BG1 Z=384, 10 iterations: direct ahead of staged copies
+// by 10% at 1 round and 8% at 4, level at 13.5, 1% behind at 27).
+constexpr size_t kDirectMaxRounds = 16;
 
 struct Handle {
     int device = 0;
@@ -39,6 +43,8 @@ struct Handle {
     int n_w_iters = 0;
     bool wms_ready = false;
     int schedule = NRLDPC_SCHEDULE_FLOODING;
+    int host_mode = NRLDPC_HOST_AUTO;
+    bool coherent_host = false;  // the GPU reads host memory over a coherent link (Grace C2C)
     // host-buffer pipeline: copies of chunk k+1 overlap the decode of chunk k
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_start = nullptr;
@@ -70,6 +76,7 @@ bool fill_table(const int* base, int rows, int cols, int z, int kb, CodeTable* t
             t->edge[e] = static_cast<uint32_t>(c * z + sh) | (static_cast<uint32_t>(z - sh) << 16);
             t->ebase4[e] = static_cast<uint32_t>(c * z + sh) * 4u;
             t->ethr[e] = static_cast<uint16_t>(z - sh);
+            t->eaddr[e] = make_uint2(t->ebase4[e], t->ethr[e]);
             t->edge_col[e] = static_cast<uint8_t>(c);
             t->edge_shift[e] = static_cast<uint16_t>(sh);
             e++;
@@ -171,6 +178,10 @@ int init_impl(const int* base, int rows, int cols, int kb, const nrldpc_config* 
         return NRLDPC_ERR_NO_DEVICE;
     }
     h->sm_count = prop.multiProcessorCount;
+    int uses_host_tables = 0;
+    if (cudaDeviceGetAttribute(&uses_host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables,
+                               cfg->device) == cudaSuccess)
+        h->coherent_host = uses_host_tables != 0;
     const size_t smem_limit = prop.sharedMemPerBlockOptin;
     const int z = cfg->z;
     int cpb = cfg->cw_per_cta;
@@ -219,8 +230,10 @@ int init_impl(const int* base, int rows, int cols, int kb, const nrldpc_config* 
     return NRLDPC_OK;
 }
 
+// llr_from_host: llr is the device view of pinned host memory; the kernel
+// reads it with ordinary loads instead of bulk copies.
 int decode_impl(Handle* h, const float* llr, uint8_t* packed, int n_cw, int n_iter, int early,
-                float* app, int32_t* iters, bool weighted, cudaStream_t stream) {
+                float* app, int32_t* iters, bool weighted, cudaStream_t stream, bool llr_from_host = false) {
     if (!h || n_cw < 0 || n_iter < 1 || (early != 0 && early != 1)) return NRLDPC_ERR_INVALID_ARG;
     if (n_cw == 0) return NRLDPC_OK;  // empty batch: nothing to read or write
     if (!llr || !packed) return NRLDPC_ERR_INVALID_ARG;
@@ -242,6 +255,7 @@ int decode_impl(Handle* h, const float* llr, uint8_t* packed, int n_cw, int n_it
     a.n_w_iters = h->n_w_iters;
     a.early_stop = early;
     a.alpha = h->alpha;
+    a.llr_from_host = llr_from_host ? 1 : 0;
     const int grid = std::min(a.n_groups, h->max_grid);
     cudaError_t e = cudaMemsetAsync(h->scratch, 0, sizeof(int), stream);
     if (e != cudaSuccess) return NRLDPC_ERR_CUDA;
@@ -254,11 +268,37 @@ int decode_impl(Handle* h, const float* llr, uint8_t* packed, int n_cw, int n_it
 // (1, 2, 4, ... rounds of max_grid * cpb codewords): chunk k+1's host->device
 // copy runs on the handle's copy stream while chunk k decodes on the caller's
 // stream, and each chunk's packed bits go back as soon as it is decoded.
+// Device view of a pinned (cudaHostAlloc'd or registered) host buffer, or
+// null when the GPU cannot address it.
+void* pinned_device_view(const void* p) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();  // clear the error of an unknown pointer
+        return nullptr;
+    }
+    if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+    // the view of p itself (the attributes describe p's allocation at p)
+    return at.devicePointer;
+}
+
 int host_decode(Handle* h, const void* h_llr, int qtype, float scale, uint8_t* h_packed, int n_cw, int n_iter,
                 int early, cudaStream_t s) {
+    const size_t round = static_cast<size_t>(h->max_grid) * h->cpb;
+    // fp32 buffers the GPU can address: DIRECT decodes the batch straight
+    // from host memory; AUTO does so on a coherent link up to
+    // kDirectMaxRounds CTA rounds (beyond that the per-group wait for host
+    // memory costs more than the staged copies do)
+    if (qtype == 0 && h->host_mode != NRLDPC_HOST_COPY) {
+        const float* d_in = static_cast<const float*>(pinned_device_view(h_llr));
+        uint8_t* d_out = static_cast<uint8_t*>(pinned_device_view(h_packed));
+        const bool usable = d_in && d_out && reinterpret_cast<uintptr_t>(d_in) % 16 == 0;
+        if (h->host_mode == NRLDPC_HOST_DIRECT && !usable) return NRLDPC_ERR_INVALID_ARG;
+        if (usable && (h->host_mode == NRLDPC_HOST_DIRECT ||
+                       (h->coherent_host && static_cast<size_t>(n_cw) <= kDirectMaxRounds * round)))
+            return decode_impl(h, d_in, d_out, n_cw, n_iter, early, nullptr, nullptr, false, s, true);
+    }
     const size_t n_bp = static_cast<size_t>(h->tab.n_bp);
     const size_t in_elem = qtype == 0 ? 4 : (qtype == 1 ? 2 : 1);
-    const size_t round = static_cast<size_t>(h->max_grid) * h->cpb;
     void* stage_in = qtype == 0 ? static_cast<void*>(h->stage_llr) : h->stage_q;
     // the copy stream must not overwrite staging a previous call still reads
     if (cudaEventRecord(h->ev_start, s) != cudaSuccess ||
@@ -467,6 +507,14 @@ int nrldpc_decode_host_async_q(nrldpc_handle* handle, const void* h_llr_q, int q
     }
     return host_decode(h, h_llr_q, qtype, scale, h_packed, n_cw, n_iter, early_stop,
                        reinterpret_cast<cudaStream_t>(stream));
+}
+
+int nrldpc_set_host_transfer(nrldpc_handle* handle, int mode) {
+    Handle* h = reinterpret_cast<Handle*>(handle);
+    if (!h || (mode != NRLDPC_HOST_AUTO && mode != NRLDPC_HOST_COPY && mode != NRLDPC_HOST_DIRECT))
+        return NRLDPC_ERR_INVALID_ARG;
+    h->host_mode = mode;
+    return NRLDPC_OK;
 }
 
 int nrldpc_set_schedule(nrldpc_handle* handle, int schedule) {

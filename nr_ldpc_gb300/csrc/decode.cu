@@ -152,8 +152,15 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
             addr[i] = 0;
             lv[i] = __uint_as_float(st.w);
         } else {
-            uint32_t a = s4old + tab.ebase4[e0 + i];
-            if (s >= tab.ethr[e0 + i]) a -= z4;  // column (s + V) mod Z of the edge's block
+            uint32_t a;
+            if (LAYERED) {  // one 64-bit table read per edge (measured faster here, slower in flooding)
+                const uint2 ea = tab.eaddr[e0 + i];
+                a = s4old + ea.x;
+                if (s >= ea.y) a -= z4;  // column (s + V) mod Z of the edge's block
+            } else {
+                a = s4old + tab.ebase4[e0 + i];
+                if (s >= tab.ethr[e0 + i]) a -= z4;
+            }
             addr[i] = a;
             lv[i] = lds(a);
         }
@@ -179,7 +186,7 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
             mag = __fmul_rn(wsel(wprev, i), i == oidx ? om2 : om1);
         else
             mag = i == oidx ? oa2 : oa1;
-        const float ro = __uint_as_float(__float_as_uint(mag) | ((oinfo << (24 - D + i)) & 0x80000000u));
+        const float ro = __uint_as_float(__float_as_uint(mag) ^ ((oinfo << (24 - D + i)) & 0x80000000u));
         const float q = __fsub_rn(lv[i], ro);
         keep[i] = LAYERED ? q : ro;
         const float qa = fabsf(q);
@@ -189,7 +196,7 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
             m1 = fminf(m1, qa);
             continue;
         }
-        if (qa < m1) idx = i;
+        if (!LAYERED && qa < m1) idx = i;  // layered: found below from the kept Q
         const float mx = max_nan(m1, qa);  // NaN |Q| leaves min1/min2 untouched
         m1 = fminf(m1, qa);
         m2 = fminf(m2, mx);
@@ -203,14 +210,19 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
     }
     float sfx_new = 0.0f;
     if (LAYERED) {
+        // The edge that gets min2 is any edge with |Q| == min1: the first
+        // argmin when the minimum is unique, and when it is not, min2 ==
+        // min1 and every such edge gets the same message.
 #pragma unroll
         for (int i = 0; i < D; i++) {
+            const bool at_min = fabsf(keep[i]) == m1;
+            if (at_min) idx = i;
             float mag;
             if (WEIGHTED)
-                mag = __fmul_rn(wsel(wcur, i), i == idx ? m2 : m1);
+                mag = __fmul_rn(wsel(wcur, i), at_min ? m2 : m1);
             else
-                mag = i == idx ? a2 : a1;
-            const float rn = __uint_as_float(__float_as_uint(mag) | ((rsign << (32 - D + i)) & 0x80000000u));
+                mag = at_min ? a2 : a1;
+            const float rn = __uint_as_float(__float_as_uint(mag) ^ ((rsign << (32 - D + i)) & 0x80000000u));
             const float v = __fadd_rn(keep[i], rn);
             if (i == LAST && sfx)
                 sfx_new = v;
@@ -232,7 +244,7 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
                 mag = __fmul_rn(wsel(wcur, i), i == idx ? m2 : m1);
             else
                 mag = i == idx ? a2 : a1;
-            const float rn = __uint_as_float(__float_as_uint(mag) | ((rsign << (32 - D + i)) & 0x80000000u));
+            const float rn = __uint_as_float(__float_as_uint(mag) ^ ((rsign << (32 - D + i)) & 0x80000000u));
             const float dt = __fsub_rn(rn, keep[i]);
             const float v = __fadd_rn(nv[i], dt);
             if (i == LAST && sfx)
@@ -467,7 +479,9 @@ struct WeightParam<true> {
     using type = WeightTable;
 };
 
-template <bool WEIGHTED, int MINB, bool LAYERED>
+// FROM_HOST: a.llr is pinned host memory (a separate instantiation, so the
+// device-resident kernels keep their register allocation).
+template <bool WEIGHTED, int MINB, bool LAYERED, bool FROM_HOST>
 __global__ void __launch_bounds__(kMaxThreads, MINB)
     decode_kernel(const __grid_constant__ CodeTable tab, const __grid_constant__ DecodeArgs a,
                   const __grid_constant__ typename WeightParam<WEIGHTED>::type wt) {
@@ -503,20 +517,35 @@ __global__ void __launch_bounds__(kMaxThreads, MINB)
         if (g >= a.n_groups) break;
         const int cw0 = g * cpb;
         const int n_valid = min(cpb, a.n_cw - cw0);
-        if (tid == 0) {  // core-column LLRs of each codeword into its Lold
-            fence_proxy_async();
-            mbar_arrive_expect_tx(bar, static_cast<uint32_t>(n_valid) * cf * 4u);
-            for (int k = 0; k < n_valid; k++)
-                bulk_g2s(smem_addr(buf0 + static_cast<size_t>(k) * cf), a.llr + static_cast<size_t>(cw0 + k) * n,
-                         cf * 4u, bar);
+        if constexpr (FROM_HOST) {
+            // pinned host memory: the CTA's threads read the core columns of
+            // each codeword in 16-byte pieces, up to eight in flight per
+            // thread (the suffix LLRs come with the first iteration's state
+            // fetch, as in the device-resident kernel)
+            const int core4 = cf / 4;
+            for (int k = 0; k < n_valid; k++) {
+                const float4* src = reinterpret_cast<const float4*>(a.llr + static_cast<size_t>(cw0 + k) * n);
+                float4* dst = reinterpret_cast<float4*>(buf0 + static_cast<size_t>(k) * cf);
+#pragma unroll 8
+                for (int m = tid; m < core4; m += blockDim.x) dst[m] = __ldcs(src + m);
+            }
+            __syncthreads();
+        } else {
+            if (tid == 0) {  // core-column LLRs of each codeword into its Lold
+                fence_proxy_async();
+                mbar_arrive_expect_tx(bar, static_cast<uint32_t>(n_valid) * cf * 4u);
+                for (int k = 0; k < n_valid; k++)
+                    bulk_g2s(smem_addr(buf0 + static_cast<size_t>(k) * cf),
+                             a.llr + static_cast<size_t>(cw0 + k) * n, cf * 4u, bar);
+            }
+            bool ok = mbar_wait_bounded(bar, phase);
+            if (!__syncthreads_and(ok)) {
+                if (tid == 0) atomicExch(a.error_flag, kErrLlrLoadTimeout);
+                mbar_wait_bounded(bar, phase);  // let the copy in flight land before leaving
+                return;
+            }
+            phase ^= 1u;
         }
-        bool ok = mbar_wait_bounded(bar, phase);
-        if (!__syncthreads_and(ok)) {
-            if (tid == 0) atomicExch(a.error_flag, kErrLlrLoadTimeout);
-            mbar_wait_bounded(bar, phase);  // let the copy in flight land before leaving
-            return;
-        }
-        phase ^= 1u;
         const bool slot_done = !valid_thread || slot >= n_valid;
         const size_t cw = static_cast<size_t>(cw0 + (slot_done ? 0 : slot));
         SlotOut out{a.packed + cw * tab.packed_bytes, a.app ? a.app + cw * n : nullptr,
@@ -554,7 +583,7 @@ __global__ void __launch_bounds__(kMaxThreads, 2)
         {   // code table of this item into shared memory
             const uint4* src = reinterpret_cast<const uint4*>(a.tables + item.code);
             uint4* dst = reinterpret_cast<uint4*>(stab);
-            for (int k = tid; k < static_cast<int>(sizeof(CodeTable) / 16); k += blockDim.x) dst[k] = src[k];
+            for (int k = tid; k < static_cast<int>(kBatchTableCopy / 16); k += blockDim.x) dst[k] = src[k];
         }
         __syncthreads();
         const CodeTable& tab = *stab;
@@ -594,12 +623,17 @@ size_t decode_smem_bytes(const CodeTable& tab, int cpb) {
     return kHeaderBytes + kWeightBytes + group_smem_bytes(tab, cpb);
 }
 
-template <bool W, int MINB, bool LAY>
+template <bool W, int MINB, bool LAY, bool HOST = false>
 const void* kernel_ptr() {
-    return reinterpret_cast<const void*>(&decode_kernel<W, MINB, LAY>);
+    return reinterpret_cast<const void*>(&decode_kernel<W, MINB, LAY, HOST>);
 }
 
-const void* select_kernel(bool weighted, int minb, bool layered) {
+// from_host: the unweighted kernels that read host-resident LLRs.
+const void* select_kernel(bool weighted, int minb, bool layered, bool from_host = false) {
+    if (from_host && !weighted) {
+        if (layered) return minb >= 2 ? kernel_ptr<false, 2, true, true>() : kernel_ptr<false, 1, true, true>();
+        return minb >= 2 ? kernel_ptr<false, 2, false, true>() : kernel_ptr<false, 1, false, true>();
+    }
     if (layered) {
         if (weighted) return minb >= 2 ? kernel_ptr<true, 2, true>() : kernel_ptr<true, 1, true>();
         return minb >= 2 ? kernel_ptr<false, 2, true>() : kernel_ptr<false, 1, true>();
@@ -621,9 +655,9 @@ cudaError_t decode_kernel_attributes(size_t smem) {
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
     for (int l = 0; l < 2; l++)
-        for (int w = 0; w < 2; w++)
+        for (int w = 0; w < 3; w++)  // plain, weighted, plain from host
             for (int m = 1; m <= 2; m++) {
-                cudaError_t e = cudaFuncSetAttribute(select_kernel(w != 0, m, l != 0),
+                cudaError_t e = cudaFuncSetAttribute(select_kernel(w == 1, m, l != 0, w == 2),
                                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                      static_cast<int>(smem));
                 if (e != cudaSuccess) return e;
@@ -633,10 +667,10 @@ cudaError_t decode_kernel_attributes(size_t smem) {
 
 int decode_max_ctas_per_sm(bool weighted, int minb, int threads, size_t smem) {
     int n = 1 << 30;
-    for (int l = 0; l < 2; l++) {
+    for (int l = 0; l < 4; l++) {  // both schedules, device- and host-resident LLRs
         int k = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, select_kernel(weighted, minb, l != 0), threads,
-                                                          smem) != cudaSuccess)
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, select_kernel(weighted, minb, l & 1, l >= 2),
+                                                          threads, smem) != cudaSuccess)
             return 0;
         n = k < n ? k : n;
     }
@@ -647,7 +681,8 @@ cudaError_t launch_decode(const CodeTable& tab, const DecodeArgs& args, const We
                           int threads, size_t smem, bool layered, int minb, cudaStream_t stream) {
     if (args.cpb < 1 || args.cpb > kMaxCpb) return cudaErrorInvalidValue;
     const bool weighted = weights != nullptr;
-    const void* k = select_kernel(weighted, minb, layered);
+    if (weighted && args.llr_from_host) return cudaErrorInvalidValue;
+    const void* k = select_kernel(weighted, minb, layered, args.llr_from_host != 0);
     NoWeights none{};
     void* params[3] = {const_cast<CodeTable*>(&tab), const_cast<DecodeArgs*>(&args),
                        weighted ? const_cast<WeightTable*>(weights) : static_cast<void*>(&none)};

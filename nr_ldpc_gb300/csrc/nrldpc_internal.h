@@ -43,6 +43,10 @@ struct alignas(16) CodeTable {
     uint16_t ethr[kMaxEdges];
     uint8_t edge_col[kMaxEdges];
     uint16_t edge_shift[kMaxEdges];  // V mod Z
+    // {ebase4, ethr} of each edge in one 64-bit word (the layered decoder's
+    // layout).  Last member: the mixed-batch kernel, flooding only, copies the
+    // table into shared memory up to here.
+    uint2 eaddr[kMaxEdges];
 };
 
 // Check-node state of one lifted row, kept between iterations (16 B, one
@@ -70,6 +74,7 @@ struct DecodeArgs {
     int* work_counter;      // dynamic codeword-group scheduler, zeroed per launch
     int* error_flag;        // bounded-wait failures
     int n_cw, n_iter, cpb, n_groups, n_w_iters, early_stop;
+    int llr_from_host;      // 1: llr is pinned host memory read over the host link
     float alpha;
 };
 
@@ -84,7 +89,8 @@ struct WorkItem {
     int32_t pad;
 };
 constexpr size_t kHeaderBytesBatch = 1024;  // mbarrier, item id, per-slot flags
-constexpr size_t kBatchTableBytes = (sizeof(CodeTable) + 127) / 128 * 128;
+constexpr size_t kBatchTableCopy = (offsetof(CodeTable, eaddr) + 15) / 16 * 16;
+constexpr size_t kBatchTableBytes = (kBatchTableCopy + 127) / 128 * 128;
 struct BatchDecodeArgs {
     const CodeTable* tables;
     const WorkItem* items;

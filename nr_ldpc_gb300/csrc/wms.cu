@@ -74,7 +74,7 @@ __device__ __forceinline__ void fwd_row(const CodeTable& tab, int e0, uint32_t s
     for (int i = 0; i < D; i++) {
         const float mag = __fmul_rn(w_prev[e0 + i], i == oidx ? om2 : om1);
         const uint32_t sb = (opar ^ (oq >> i)) & 1u;
-        rold[i] = __uint_as_float(__float_as_uint(mag) | (sb << 31));
+        rold[i] = __uint_as_float(__float_as_uint(mag) ^ (sb << 31));
         const float q = __fsub_rn(lv[i], rold[i]);
         if (LAYERED) rold[i] = q;  // the layered update needs Q, not R_old
         const float qa = fabsf(q);
@@ -94,7 +94,7 @@ __device__ __forceinline__ void fwd_row(const CodeTable& tab, int e0, uint32_t s
     for (int i = 0; i < D; i++) {
         const float mag = __fmul_rn(w_cur[e0 + i], i == i1 ? m2 : m1);
         const uint32_t sb = (par ^ (qmask >> i)) & 1u;
-        const float rn = __uint_as_float(__float_as_uint(mag) | (sb << 31));
+        const float rn = __uint_as_float(__float_as_uint(mag) ^ (sb << 31));
         if (LAYERED)
             lnew[addr[i]] = __fadd_rn(rold[i], rn);  // A = Q + R_new
         else

@@ -2,9 +2,10 @@
 // shaped like the reference's test_throughput (src/main.cpp:147-171):
 // setup_ldpc -> one Decoder per stream -> perform_gpu_ldpc_decoding on pinned
 // host buffers -> synchronize.
-//   host_decode <A> <n_iter> <llr.f32> <out.u8>
+//   host_decode <A> <n_iter> <llr.f32> <out.u8> [host transfer mode]
 // reads n codewords of fp32 LLRs (file size / (4 * N_bp)) and writes their
-// packed hard decisions.
+// packed hard decisions; the mode is NRLDPC_HOST_AUTO (default), _COPY or
+// _DIRECT.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -14,8 +15,8 @@
 #include "nr_ldpc_gb300.hpp"
 
 int main(int argc, char** argv) {
-    if (argc != 5) {
-        std::fprintf(stderr, "usage: %s A n_iter llr.f32 out.u8\n", argv[0]);
+    if (argc != 5 && argc != 6) {
+        std::fprintf(stderr, "usage: %s A n_iter llr.f32 out.u8 [mode]\n", argv[0]);
         return 2;
     }
     const int A = std::atoi(argv[1]), n_iter = std::atoi(argv[2]);
@@ -33,6 +34,7 @@ int main(int argc, char** argv) {
         if (std::fread(llr, 1, static_cast<size_t>(bytes), f) != static_cast<size_t>(bytes)) return 4;
         std::fclose(f);
         nrldpc::Decoder dec(p, n_cw);
+        if (argc == 6) dec.set_host_transfer(std::atoi(argv[5]));
         cudaMallocHost(&packed, static_cast<size_t>(n_cw) * dec.packed_bytes());
         cudaStream_t stream;
         cudaStreamCreate(&stream);

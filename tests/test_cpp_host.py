@@ -41,11 +41,13 @@ def test_cpp_caller_decodes_like_the_oracle(tmp_path, cuda_lib):
     llr, _ = oc.gen_llr(22, 5150, 0, sig, 2)
     src, dst = tmp_path / "llr.f32", tmp_path / "out.u8"
     llr.tofile(src)
-    r = subprocess.run([exe, "8424", "10", str(src), str(dst)], capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr
     want, _, _ = oc.minsum_f32(llr, 10)
-    got = np.fromfile(dst, np.uint8).reshape(want.shape)
-    np.testing.assert_array_equal(got, want)
+    for mode in ([], ["0"], ["1"], ["2"]):  # default, AUTO, COPY, DIRECT host transfer
+        dst.unlink(missing_ok=True)
+        r = subprocess.run([exe, "8424", "10", str(src), str(dst), *mode], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        got = np.fromfile(dst, np.uint8).reshape(want.shape)
+        np.testing.assert_array_equal(got, want)
 
 
 @pytest.mark.gpu

@@ -231,6 +231,7 @@ def test_host_call_in_chunks_back_to_back(gpu):
     back to back on one stream with different inputs both come out right."""
     n = 1500  # 304-codeword rounds at BG1 Z=384: chunks of 304, 608, 588
     dec = Decoder(bg=1, z=384, max_batch=n)
+    dec.set_host_transfer("copy")
     sig = torch.full((n,), codes.noise_sigma(1.6, 1 / 3), device=gpu)
     llr_a, _ = dec.gen_llr(41, 0, sig)
     llr_b, _ = dec.gen_llr(42, 0, sig)
@@ -248,6 +249,36 @@ def test_host_call_in_chunks_back_to_back(gpu):
     dec.decode_host_q(q.pin_memory(), out_q, 7, stream=s)
     s.synchronize()
     assert torch.equal(out_q, dec.decode(q.to(gpu).float(), 7).cpu())
+
+
+@pytest.mark.parametrize("bg,z,n,early", [(1, 384, 700, False), (2, 52, 333, True)])
+def test_host_transfer_modes_agree(gpu, bg, z, n, early):
+    """'direct' (the decoder reads pinned host LLRs and writes the packed bits
+    back itself), 'copy' (staged chunks) and 'auto' all give the device
+    call's bits, also from views into the middle of pinned buffers; 'direct'
+    refuses pageable buffers."""
+    dec = Decoder(bg=bg, z=z, max_batch=n)
+    sig = torch.full((n,), codes.noise_sigma(1.7, dec.kb / (dec.cols - 2)), device=gpu)
+    llr, _ = dec.gen_llr(61, 0, sig)
+    ref = dec.decode(llr, 8, early_stop=early).cpu()
+    h_llr = llr.cpu().pin_memory()
+    s = torch.cuda.Stream()
+    for mode in ("direct", "copy", "auto"):
+        dec.set_host_transfer(mode)
+        out = torch.full((n, dec.packed_bytes), 0xAB, dtype=torch.uint8).pin_memory()
+        dec.decode_host(h_llr, out, 8, early_stop=early, stream=s)
+        s.synchronize()
+        assert torch.equal(out, ref), mode
+        out.fill_(0xAB)
+        dec.decode_host(h_llr[3:], out[3:], 8, early_stop=early, stream=s)
+        s.synchronize()
+        assert torch.equal(out[3:], ref[3:]) and (out[:3] == 0xAB).all(), mode
+    dec.set_host_transfer("direct")
+    with pytest.raises(_lib.NrLdpcError) as e:
+        dec.decode_host(llr.cpu(), torch.empty((n, dec.packed_bytes), dtype=torch.uint8), 8, stream=s)
+    assert e.value.status == -1
+    with pytest.raises(_lib.NrLdpcError):
+        dec.set_host_transfer(3)
 
 
 def test_posterior_within_1e5_of_fp64_transcription(gpu):

@@ -73,6 +73,31 @@ def test_weighted_decode_with_early_stop_matches_oracle(gpu, bg, z):
     np.testing.assert_array_equal(app.cpu().numpy().view(np.uint32), oapp.view(np.uint32))
 
 
+@pytest.mark.parametrize("layered", [False, True])
+def test_signed_weights_match_oracle(gpu, layered):
+    """Negative and zero weights: every message is the product w * sign * min,
+    as the oracle computes it."""
+    n, T = 10, 6
+    oc, llr, _ = _data(1, 64, n, 8, ebn0=2.0)
+    rng = np.random.default_rng(9)
+    w = rng.uniform(-0.9, 0.95, (T, oc.n_edges)).astype(np.float32)
+    w[:, ::17] = 0.0
+    dec = Decoder(bg=1, z=64, max_batch=n)
+    if layered:
+        dec.set_schedule("layered")
+    dec.set_weights(w)
+    pk, app, its = dec.decode(torch.from_numpy(llr).to(gpu), T, early_stop=True, weighted=True,
+                              want_app=True, want_iters=True)
+    torch.cuda.synchronize()
+    if layered:
+        opk, oapp, oits = oc.layered_f32(llr, T, w=w, early_stop=True, want_app=True)
+    else:
+        opk, oapp, oits = oc.wms_decode_f32(llr, T, w, early_stop=True, want_app=True)
+    np.testing.assert_array_equal(its.cpu().numpy(), oits)
+    np.testing.assert_array_equal(pk.cpu().numpy(), opk)
+    np.testing.assert_array_equal(app.cpu().numpy().view(np.uint32), oapp.view(np.uint32))
+
+
 def test_adam_step_matches_numpy(gpu):
     tr = Trainer(bg=2, z=8, n_iter=2, batch=4, chunk=4, lr=1e-2)
     rng = np.random.default_rng(0)
