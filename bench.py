@@ -227,12 +227,13 @@ def learned_vs_plain(dec, stream, batch: int, ebn0: float = 1.8, frames: int = 6
                 "info_gbps": batch * K_INFO / (ms * 1e-3) / 1e9, "ms_per_batch": ms}
 
     plain = run("flooding", None, ITERS)
-    learned = None
+    learned, tried = None, []
     for cap in (4, 5, 6):
         learned = run("layered", "bg1_L6", cap)
+        tried.append({k: learned[k] for k in ("iters_max", "fer", "fer_ci95", "avg_iters", "info_gbps")})
         if learned["fer"] <= plain["fer"]:
             break
-    res = {"ebn0_db": ebn0, "early_stop": True, "plain": plain, "learned": learned,
+    res = {"ebn0_db": ebn0, "early_stop": True, "plain": plain, "learned": learned, "learned_caps_tried": tried,
            "learned_matches_plain_fer": learned["fer"] <= plain["fer"],
            "speedup": learned["info_gbps"] / plain["info_gbps"],
            "layered_without_weights": run("layered", None, learned["iters_max"]),
@@ -302,8 +303,16 @@ def training_step(steps: int = 5):
         tr.step()
     torch.cuda.synchronize()
     ms = 1e3 * (time.perf_counter() - t0) / steps
+    # roofline model of a training step: forward + recompute + adjoint as three
+    # times the forward's algorithmic bytes (4 N_bp + N_bp/8 + I 8 (E_Z + N_bp))
+    n_bp, e_z, iters = 52 * 128, 197 * 128, 8
+    step_bytes = 3 * (4 * n_bp + n_bp // 8 + iters * 8 * (e_z + n_bp)) * 16384
+    peak, peak_kind = measured_peaks()
+    achieved = step_bytes / (ms * 1e-3) / 1e9
     return {"config": "BG2 Z=128, 8 iterations, 16384 codewords/step, Adam 1e-3", "ms_per_step": ms,
-            "codewords_per_s": 16384 / (ms * 1e-3), "steps_timed": steps}
+            "codewords_per_s": 16384 / (ms * 1e-3), "steps_timed": steps,
+            "model_bytes_per_step": step_bytes, "achieved_gbs": achieved,
+            "frac": achieved / peak, "peak_gbs": peak, "peak_kind": peak_kind}
 
 
 def c1_fer_curve(dec, batch: int = 4096):

@@ -22,8 +22,9 @@ const int kBaseZ[8] = {2, 3, 5, 7, 9, 11, 13, 15};
 constexpr int kHostChunks = 16;  // most chunks of one host-buffer decode
 // Largest batch, in CTA rounds, that NRLDPC_HOST_AUTO decodes straight from
 // host memory (GB300, BG1 Z=384, 10 iterations: direct ahead of staged copies
-// by 10% at 1 round and 8% at 4, level at 13.5, 1% behind at 27).
-constexpr size_t kDirectMaxRounds = 16;
+// by 10% at 1 round and 8% at 4, 1% behind to 2% ahead at 13.5 depending on
+// the run, 1% behind at 27).
+constexpr size_t kDirectMaxRounds = 8;
 
 struct Handle {
     int device = 0;
