@@ -33,7 +33,7 @@ def reduce_counts(counts, group=None) -> torch.Tensor:
 
 
 def max_over_ranks(value: float, device=None, group=None) -> float:
-    """Largest value over ranks (the step time the job is judged on)."""
+    """Largest value over ranks (the whole job's step time is its slowest rank's)."""
     if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size(group) == 1:
         return float(value)
     t = torch.tensor([float(value)], dtype=torch.float64, device=device)
