@@ -197,14 +197,18 @@ int nrldpc_count_errors(nrldpc_handle* h, const uint8_t* d_packed, const uint8_t
 /* ---- mixed-code batches (no reference counterpart; the reference compiles
  * in one base graph and one Z per process, src/globals.h:15) ----------------
  * A job is one codeword of any 5G NR (bg, z), optionally rate matched
- * (3GPP TS 38.212 5.4.2.1 bit selection, full circular buffer, BPSK so no
- * interleaver) with filler bits.  All offsets index caller buffers. */
+ * (3GPP TS 38.212 5.4.2.1 bit selection from a full circular buffer, then the
+ * 5.4.2.2 bit interleaver for modulation order qm) with filler bits.  The
+ * rate-matched LLRs are in transmission order.  All offsets index caller
+ * buffers. */
 typedef struct {
     int32_t bg, z;        /* base graph 1|2 and lifting size */
     int32_t k_prime;      /* information bits before filler; 0 = kb*Z (no filler) */
-    int32_t e;            /* rate-matched length; 0 = one pass over the buffer */
+    int32_t e;            /* rate-matched length (a multiple of qm); 0 = one pass over the buffer */
     int32_t rv;           /* redundancy version 0..3 */
     float sigma;          /* noise std-dev (channel generator only) */
+    int32_t qm;           /* modulation order 1, 2, 4, 6, 8 or 10 (bit interleaver); 0 = 1 */
+    int32_t reserved;     /* 0 */
     int64_t llr_offset;   /* float offset of the mother-code LLRs [cols*Z], multiple of 4 */
     int64_t e_offset;     /* float offset of the rate-matched LLRs [e] */
     int64_t out_offset;   /* byte offset of the packed hard decisions / codeword */
@@ -222,11 +226,14 @@ int nrldpc_batch_get_cw_per_cta(nrldpc_batch* b, int bg, int z, int* cw_per_cta)
  * work queue (largest work first).  Synchronous. */
 int nrldpc_batch_set_jobs(nrldpc_batch* b, const nrldpc_job* jobs, int n_jobs);
 /* Seeded rate-matched transmissions of the loaded jobs (bit-identical to the
- * oracle): d_llr_e at e_offset, transmitted codewords at out_offset of d_cw. */
+ * oracle): every bit on the wire (after the bit interleaver) through BPSK and
+ * AWGN, d_llr_e at e_offset in transmission order, transmitted codewords at
+ * out_offset of d_cw. */
 int nrldpc_batch_gen(nrldpc_batch* b, uint64_t seed, uint64_t cw_base, float* d_llr_e,
                      uint8_t* d_cw, nrldpc_stream_t stream);
-/* De-rate-matching: rate-matched LLRs -> mother-code LLRs at llr_offset
- * (punctured/unsent 0, filler +inf, repetitions added in order). */
+/* De-rate-matching: rate-matched LLRs in transmission order -> de-interleaved
+ * -> mother-code LLRs at llr_offset (punctured/unsent 0, filler +inf,
+ * repetitions added in rate-matching order). */
 int nrldpc_batch_derate(nrldpc_batch* b, const float* d_llr_e, float* d_llr, nrldpc_stream_t stream);
 /* Decode all loaded jobs in one persistent launch (device work queue),
  * replayed from a CUDA graph; d_iters (may be NULL) indexed by job. */

@@ -16,14 +16,16 @@ from .codes import BG_SHAPE, KB_MAX
 from .decoder import _dev_ptr, _stream_ptr
 
 JOB_DTYPE = np.dtype([("bg", "<i4"), ("z", "<i4"), ("k_prime", "<i4"), ("e", "<i4"), ("rv", "<i4"),
-                      ("sigma", "<f4"), ("llr_offset", "<i8"), ("e_offset", "<i8"),
-                      ("out_offset", "<i8")])
-assert JOB_DTYPE.itemsize == 48
+                      ("sigma", "<f4"), ("qm", "<i4"), ("reserved", "<i4"), ("llr_offset", "<i8"),
+                      ("e_offset", "<i8"), ("out_offset", "<i8")])
+assert JOB_DTYPE.itemsize == 56
 
 
-def make_jobs(bg, z, k_prime=0, e=0, rv=0, sigma=1.0):
+def make_jobs(bg, z, k_prime=0, e=0, rv=0, sigma=1.0, qm=1):
     """Job array with contiguous layouts: mother LLRs (4-float aligned),
-    rate-matched LLRs, packed outputs.  Returns (jobs, n_llr, n_e, n_out)."""
+    rate-matched LLRs, packed outputs.  qm: modulation order of the bit
+    interleaver (e must be a multiple of it).  Returns (jobs, n_llr, n_e,
+    n_out)."""
     bg = np.asarray(bg, np.int32)
     n = bg.size
     z = np.broadcast_to(np.asarray(z, np.int32), (n,))
@@ -32,6 +34,7 @@ def make_jobs(bg, z, k_prime=0, e=0, rv=0, sigma=1.0):
     jobs["k_prime"] = np.broadcast_to(k_prime, (n,))
     jobs["rv"] = np.broadcast_to(rv, (n,))
     jobs["sigma"] = np.broadcast_to(sigma, (n,))
+    jobs["qm"] = np.broadcast_to(qm, (n,))
     cols = np.where(bg == 1, BG_SHAPE[1][1], BG_SHAPE[2][1])
     kb = np.where(bg == 1, KB_MAX[1], KB_MAX[2])
     nbp = cols * z

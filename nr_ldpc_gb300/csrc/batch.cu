@@ -34,6 +34,8 @@ struct PlanDev {
     uint8_t step_col[kMaxRows];
 };
 
+static_assert(sizeof(nrldpc_job) == 56, "nrldpc_job layout (mirrored by the Python binding)");
+
 // Rate-matching geometry of one job, resolved on the host.
 struct JobDev {
     int32_t code;
@@ -41,7 +43,7 @@ struct JobDev {
     int32_t e;         // transmitted bits
     int32_t k0;        // start in the circular buffer
     float sigma;
-    int32_t pad;
+    int32_t qm;        // modulation order of the bit interleaver (1: none)
     int64_t llr_offset, e_offset, out_offset;
 };
 
@@ -90,7 +92,19 @@ struct GenBatchArgs {
     int n_jobs;
 };
 
-// One CTA per job: info bits, encode, select e bits from k0, BPSK + AWGN.
+// Bit interleaver of TS 38.212 5.4.2.2, f[i + j*Qm] = e[i*E/Qm + j]: the e
+// index of the bit sent at position p, and the position of e index k.
+__device__ __forceinline__ int il_src(int e, int qm, int p) {
+    return qm == 1 ? p : (p % qm) * (e / qm) + p / qm;
+}
+__device__ __forceinline__ int il_pos(int e, int qm, int k) {
+    if (qm == 1) return k;
+    const int rows = e / qm;
+    return k / rows + (k % rows) * qm;
+}
+
+// One CTA per job: info bits, encode, select e bits from k0, interleave,
+// BPSK + AWGN per transmitted position.
 __global__ void __launch_bounds__(256) batch_gen_kernel(const __grid_constant__ GenBatchArgs g) {
     extern __shared__ uint8_t x[];  // [n_bp] codeword bits, then [z] scratch
     const uint32_t k0s = static_cast<uint32_t>(g.seed), k1s = static_cast<uint32_t>(g.seed >> 32);
@@ -130,9 +144,9 @@ __global__ void __launch_bounds__(256) batch_gen_kernel(const __grid_constant__ 
             float gs[4];
             dev::gauss4(o, gs);
             for (int q = 0; q < 4 && 4 * t + q < jb.e; q++) {
-                const int k = 4 * t + q;
-                const int j = 2 * z + rm_index(z, ncb, K, jb.k_prime, jb.k0, k);
-                out[k] = dev::bpsk_llr(x[j], gs[q], sg, s2);
+                const int p = 4 * t + q;
+                const int j = 2 * z + rm_index(z, ncb, K, jb.k_prime, jb.k0, il_src(jb.e, jb.qm, p));
+                out[p] = dev::bpsk_llr(x[j], gs[q], sg, s2);
             }
         }
         __syncthreads();
@@ -148,8 +162,8 @@ struct DerateArgs {
 };
 
 // One CTA per job.  Each non-filler position c of the compressed buffer
-// collects bits k = k_first, k_first + Nc, ... (< e) in order; the first copy
-// is taken as is, later copies added.
+// collects bits k = k_first, k_first + Nc, ... (< e) in order, each read from
+// its interleaved position; the first copy is taken as is, later copies added.
 __global__ void __launch_bounds__(256) batch_derate_kernel(const __grid_constant__ DerateArgs a) {
     for (int i = blockIdx.x; i < a.n_jobs; i += gridDim.x) {
         const JobDev jb = a.jobs[i];
@@ -165,8 +179,8 @@ __global__ void __launch_bounds__(256) batch_derate_kernel(const __grid_constant
             const int kf = (c - c0 + nc) % nc;
             float v = 0.0f;
             if (kf < jb.e) {
-                v = in[kf];
-                for (int k = kf + nc; k < jb.e; k += nc) v = __fadd_rn(v, in[k]);
+                v = in[il_pos(jb.e, jb.qm, kf)];
+                for (int k = kf + nc; k < jb.e; k += nc) v = __fadd_rn(v, in[il_pos(jb.e, jb.qm, k)]);
             }
             out[2 * z + (c < f0 ? c : c + nf)] = v;
         }
@@ -380,13 +394,17 @@ int nrldpc_batch_set_jobs(nrldpc_batch* batch, const nrldpc_job* jobs, int n_job
         const CodeTable& t = b->h_tables[id];
         const int K = t.kb * t.z, ncb = t.n_bp - 2 * t.z;
         const int kp = j.k_prime ? j.k_prime : K;
+        const int qm = j.qm ? j.qm : 1;
+        const int e = j.e ? j.e : ncb - (K - kp);
         if (kp <= 2 * t.z || kp > K || j.e < 0 || j.rv < 0 || j.rv > 3 || j.llr_offset < 0 ||
-            j.llr_offset % 4 != 0 || j.e_offset < 0 || j.out_offset < 0)
+            j.llr_offset % 4 != 0 || j.e_offset < 0 || j.out_offset < 0 ||
+            (qm != 1 && qm != 2 && qm != 4 && qm != 6 && qm != 8 && qm != 10) || e % qm != 0)
             return NRLDPC_ERR_INVALID_ARG;
         JobDev& d = b->h_jobs[i];
         d.code = id;
         d.k_prime = kp;
-        d.e = j.e ? j.e : ncb - (K - kp);
+        d.e = e;
+        d.qm = qm;
         d.k0 = rm_k0(j.bg, t.z, j.rv);
         d.sigma = j.sigma;
         d.llr_offset = j.llr_offset;

@@ -593,8 +593,17 @@ int orc_rm_index(int z, int ncb, int kb_z, int k_prime, int k0, int k) {
     return c < f0 ? c : c + nf;
 }
 
+/* TS 38.212 5.4.2.2: f_{i + j*Qm} = e_{i*E/Qm + j}.  Inverse of position p:
+ * i = p mod Qm, j = p div Qm. */
+int orc_interleave_src(int e, int qm, int p) {
+    if (qm <= 1) return p;
+    return (p % qm) * (e / qm) + p / qm;
+}
+
+static int valid_qm(int q) { return q == 1 || q == 2 || q == 4 || q == 6 || q == 8 || q == 10; }
+
 int orc_gen_rm_llr(const orc_code* c, int kb, int bg, uint64_t seed, uint64_t cw_base, int n_cw,
-                   const float* sigma, const int* k_prime, const int* e, const int* rv,
+                   const float* sigma, const int* k_prime, const int* e, const int* rv, const int* qm,
                    int e_stride, float* llr_e, uint8_t* cw_packed) {
     const int z = c->z, N = c->cols * z, K = kb * z, ncb = N - 2 * z;
     const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
@@ -604,7 +613,8 @@ int orc_gen_rm_llr(const orc_code* c, int kb, int bg, uint64_t seed, uint64_t cw
     for (int i = 0; i < n_cw && !rc; i++) {
         const uint64_t id = cw_base + (uint64_t)i;
         const int kp = k_prime[i] > 0 ? k_prime[i] : K;
-        if (kp > K || kp < 2 * z || e[i] > e_stride || e[i] < 1) { rc = -1; break; }
+        const int q = qm && qm[i] > 0 ? qm[i] : 1;
+        if (kp > K || kp < 2 * z || e[i] > e_stride || e[i] < 1 || !valid_qm(q) || e[i] % q) { rc = -1; break; }
         for (int blk = 0; blk * 128 < K; blk++) {
             uint32_t ctr[4] = {(uint32_t)blk, (uint32_t)id, (uint32_t)(id >> 32), 1u}, o[4];
             orc_philox4x32(ctr, key, o);
@@ -633,15 +643,16 @@ int orc_gen_rm_llr(const orc_code* c, int kb, int bg, uint64_t seed, uint64_t cw
                 g[2 * h] = rad * cs;
                 g[2 * h + 1] = rad * sn;
             }
-            for (int q = 0; q < 4 && 4 * t + q < e[i]; q++) {
-                const int k = 4 * t + q;
+            for (int h = 0; h < 4 && 4 * t + h < e[i]; h++) {
+                const int p = 4 * t + h; /* transmitted position */
+                const int k = orc_interleave_src(e[i], q, p);
                 const int j = 2 * z + orc_rm_index(z, ncb, K, kp, k0, k);
                 const int bit = (cwp[j >> 3] >> (j & 7)) & 1;
                 const float x = bit ? -1.0f : 1.0f;
-                const float ns = g[q] * sg;
+                const float ns = g[h] * sg;
                 const float y = x + ns;
                 const float y2 = y * 2.0f;
-                out[k] = y2 / s2;
+                out[p] = y2 / s2;
             }
         }
     }
@@ -650,12 +661,16 @@ int orc_gen_rm_llr(const orc_code* c, int kb, int bg, uint64_t seed, uint64_t cw
 }
 
 int orc_derate_match(const orc_code* c, int kb, int bg, int n_cw, const float* llr_e, int e_stride,
-                     const int* k_prime, const int* e, const int* rv, float* llr) {
+                     const int* k_prime, const int* e, const int* rv, const int* qm, float* llr) {
     const int z = c->z, N = c->cols * z, K = kb * z, ncb = N - 2 * z;
     uint8_t* seen = (uint8_t*)malloc(N);
     for (int i = 0; i < n_cw; i++) {
         const int kp = k_prime[i] > 0 ? k_prime[i] : K;
-        if (kp > K || kp < 2 * z || e[i] > e_stride || e[i] < 1) { free(seen); return -1; }
+        const int q = qm && qm[i] > 0 ? qm[i] : 1;
+        if (kp > K || kp < 2 * z || e[i] > e_stride || e[i] < 1 || !valid_qm(q) || e[i] % q) {
+            free(seen);
+            return -1;
+        }
         const int k0 = orc_rm_k0(bg, z, rv[i]);
         float* out = llr + (size_t)i * N;
         for (int j = 0; j < N; j++) out[j] = 0.0f;
@@ -663,7 +678,9 @@ int orc_derate_match(const orc_code* c, int kb, int bg, int n_cw, const float* l
         memset(seen, 0, N);
         for (int k = 0; k < e[i]; k++) {
             const int j = 2 * z + orc_rm_index(z, ncb, K, kp, k0, k);
-            const float v = llr_e[(size_t)i * e_stride + k];
+            /* position of e_k on the wire: k = i*E/Qm + jj -> p = i + jj*Qm */
+            const int p = q == 1 ? k : (k / (e[i] / q)) + (k % (e[i] / q)) * q;
+            const float v = llr_e[(size_t)i * e_stride + p];
             if (seen[j]) out[j] = out[j] + v;
             else { out[j] = v; seen[j] = 1; }
         }

@@ -72,20 +72,27 @@ int orc_gen_llr(const orc_code* c, int kb, uint64_t seed, uint64_t cw_base, int 
  * Mother codeword x[cols*Z]; circular buffer d[j] = x[2Z + j], Ncb = cols*Z - 2Z
  * (full buffer); filler bits x[k_prime .. kb*Z) are NULL (never sent, known 0).
  * k0 from rv as the standard's table; E bits e_k = d[(k0 + j) mod Ncb] taken in
- * order skipping NULLs.  BPSK, so no bit interleaving. */
+ * order skipping NULLs; then the bit interleaver of 5.4.2.2 for modulation
+ * order Qm (E a multiple of Qm): f[i + j*Qm] = e[i*E/Qm + j], i < Qm,
+ * j < E/Qm.  Qm = 1 (or 0) leaves the order as it is.  Every transmitted bit
+ * goes through BPSK + AWGN here, so Qm only fixes the bit order on the wire. */
 int orc_rm_k0(int bg, int z, int rv);
+/* e index of the bit sent at position p (f_p = e_k) for length e, order qm. */
+int orc_interleave_src(int e, int qm, int p);
 /* d index (0 .. Ncb-1) of rate-matched bit k. */
 int orc_rm_index(int z, int ncb, int kb_z, int k_prime, int k0, int k);
 /* Seeded rate-matched transmission: info bits (k_prime random, filler 0),
- * encode, select e bits, BPSK + AWGN sigma[i]; llr_e [n_cw][e_stride]. */
+ * encode, select e bits, interleave for qm[i] (NULL: 1), BPSK + AWGN sigma[i]
+ * per transmitted position; llr_e [n_cw][e_stride] in transmission order. */
 int orc_gen_rm_llr(const orc_code* c, int kb, int bg, uint64_t seed, uint64_t cw_base, int n_cw,
-                   const float* sigma, const int* k_prime, const int* e, const int* rv,
+                   const float* sigma, const int* k_prime, const int* e, const int* rv, const int* qm,
                    int e_stride, float* llr_e, uint8_t* cw_packed);
 /* Receiver: rate-matched LLRs -> mother-code LLRs [n_cw][cols*Z]: punctured
- * and unsent columns 0, filler +inf, repeated bits added in transmission
- * order (first copy taken as is). */
+ * and unsent columns 0, filler +inf, repeated bits added in rate-matching
+ * order (first copy taken as is); llr_e in transmission order for qm[i]
+ * (NULL: 1), de-interleaved first. */
 int orc_derate_match(const orc_code* c, int kb, int bg, int n_cw, const float* llr_e, int e_stride,
-                     const int* k_prime, const int* e, const int* rv, float* llr);
+                     const int* k_prime, const int* e, const int* rv, const int* qm, float* llr);
 
 /* ---- CRC (3GPP TS 38.212 5.1), bitwise long division ------------------------
  * poly: generator without the leading term (CRC24A 0x864CFB, CRC24B 0x800063,

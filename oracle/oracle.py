@@ -73,10 +73,11 @@ def lib():
         L.orc_crc.argtypes = [_u8p, C.c_int, C.c_uint32, C.c_int]
         L.orc_rm_k0.argtypes = [C.c_int, C.c_int, C.c_int]
         L.orc_rm_index.argtypes = [C.c_int] * 6
+        L.orc_interleave_src.argtypes = [C.c_int, C.c_int, C.c_int]
         L.orc_gen_rm_llr.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_uint64, C.c_uint64, C.c_int,
-                                     _f32p, _i32p, _i32p, _i32p, C.c_int, _f32p, C.c_void_p]
+                                     _f32p, _i32p, _i32p, _i32p, _i32p, C.c_int, _f32p, C.c_void_p]
         L.orc_derate_match.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _f32p, C.c_int,
-                                       _i32p, _i32p, _i32p, _f32p]
+                                       _i32p, _i32p, _i32p, _i32p, _f32p]
         _lib = L
     return _lib
 
@@ -211,30 +212,37 @@ def rm_index(z, ncb, kb_z, k_prime, k0, k):
     return lib().orc_rm_index(z, ncb, kb_z, k_prime, k0, k)
 
 
-def gen_rm_llr(oc, kb, bg, seed, cw_base, sigma, k_prime, e, rv):
+def interleave_src(e, qm, p):
+    """e index of the bit sent at position p (TS 38.212 5.4.2.2)."""
+    return lib().orc_interleave_src(int(e), int(qm), int(p))
+
+
+def gen_rm_llr(oc, kb, bg, seed, cw_base, sigma, k_prime, e, rv, qm=1):
     sigma = np.ascontiguousarray(np.atleast_1d(sigma), np.float32)
     n = sigma.shape[0]
     kp = np.ascontiguousarray(np.broadcast_to(k_prime, (n,)), np.int32)
     ee = np.ascontiguousarray(np.broadcast_to(e, (n,)), np.int32)
     rr = np.ascontiguousarray(np.broadcast_to(rv, (n,)), np.int32)
+    qq = np.ascontiguousarray(np.broadcast_to(qm, (n,)), np.int32)
     stride = int(ee.max())
     llr_e = np.zeros((n, stride), np.float32)
     cw = np.zeros((n, oc.n_bytes), np.uint8)
-    rc = lib().orc_gen_rm_llr(oc._h, kb, bg, int(seed), int(cw_base), n, sigma, kp, ee, rr, stride,
+    rc = lib().orc_gen_rm_llr(oc._h, kb, bg, int(seed), int(cw_base), n, sigma, kp, ee, rr, qq, stride,
                               llr_e, _ptr(cw))
     if rc:
         raise RuntimeError(f"orc_gen_rm_llr rc={rc}")
     return llr_e, cw
 
 
-def derate_match(oc, kb, bg, llr_e, k_prime, e, rv):
+def derate_match(oc, kb, bg, llr_e, k_prime, e, rv, qm=1):
     llr_e = np.ascontiguousarray(llr_e, np.float32)
     n, stride = llr_e.shape
     kp = np.ascontiguousarray(np.broadcast_to(k_prime, (n,)), np.int32)
     ee = np.ascontiguousarray(np.broadcast_to(e, (n,)), np.int32)
     rr = np.ascontiguousarray(np.broadcast_to(rv, (n,)), np.int32)
+    qq = np.ascontiguousarray(np.broadcast_to(qm, (n,)), np.int32)
     out = np.zeros((n, oc.n_bp), np.float32)
-    rc = lib().orc_derate_match(oc._h, kb, bg, n, llr_e, stride, kp, ee, rr, out)
+    rc = lib().orc_derate_match(oc._h, kb, bg, n, llr_e, stride, kp, ee, rr, qq, out)
     if rc:
         raise RuntimeError(f"orc_derate_match rc={rc}")
     return out

@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 import torch
 
-from nr_ldpc_gb300 import Decoder, codes
+from nr_ldpc_gb300 import Decoder, _lib, codes
 from nr_ldpc_gb300.batch import Batch, make_jobs
 from oracle import oracle as O
 
@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 ZS = (64, 96, 128, 192, 256, 320, 384)
 
 
-def _mix(n, seed, zs=ZS, small=False):
+def _mix(n, seed, zs=ZS, small=False, qms=(1,)):
     rng = np.random.default_rng(seed)
     bg = rng.integers(1, 3, n)
     z = rng.choice(zs, n)
@@ -26,10 +26,12 @@ def _mix(n, seed, zs=ZS, small=False):
     rv = rng.choice([0, 0, 0, 1, 2, 3], n)
     ncb = np.where(bg == 1, 66, 50) * z
     e = np.where(rv > 0, np.maximum(e, ncb), e)  # retransmission versions: cover the buffer
+    qm = rng.choice(qms, n)
+    e = (e + qm - 1) // qm * qm  # a whole number of modulation symbols
     eb = rng.uniform(1.0, 3.0, n)
     rate_eff = kp / e
     sigma = np.sqrt((1.0 / rate_eff) / (2.0 * 10 ** (eb / 10))).astype(np.float32)
-    return make_jobs(bg, z, kp, e, rv, sigma)
+    return make_jobs(bg, z, kp, e, rv, sigma, qm)
 
 
 def _oracle(bg, z):
@@ -37,7 +39,11 @@ def _oracle(bg, z):
 
 
 def test_generate_derate_decode_against_oracle(gpu):
-    jobs, n_llr, n_e, n_out = _mix(24, 3)
+    """Every job bit-exact with the oracle through generation (rate matching,
+    bit interleaving for modulation orders 1-10, channel), de-rate-matching
+    and decoding."""
+    jobs, n_llr, n_e, n_out = _mix(30, 3, qms=(1, 2, 4, 6, 8, 10))
+    assert len(set(jobs["qm"].tolist())) == 6
     b = Batch(max_jobs=64)
     b.set_jobs(jobs)
     llr_e = torch.zeros(n_e, device=gpu)
@@ -56,15 +62,26 @@ def test_generate_derate_decode_against_oracle(gpu):
         oc = _oracle(bg, z)
         kb = codes.KB_MAX[bg]
         e = int(j["e"])
-        le, c = O.gen_rm_llr(oc, kb, bg, 99, 5000 + i, j["sigma"], int(j["k_prime"]), e, int(j["rv"]))
+        qm = int(j["qm"])
+        le, c = O.gen_rm_llr(oc, kb, bg, 99, 5000 + i, j["sigma"], int(j["k_prime"]), e, int(j["rv"]), qm)
         np.testing.assert_array_equal(h_e[j["e_offset"]:j["e_offset"] + e].view(np.uint32), le[0].view(np.uint32))
         np.testing.assert_array_equal(h_cw[j["out_offset"]:j["out_offset"] + oc.n_bytes], c[0])
-        m = O.derate_match(oc, kb, bg, le, int(j["k_prime"]), e, int(j["rv"]))
+        m = O.derate_match(oc, kb, bg, le, int(j["k_prime"]), e, int(j["rv"]), qm)
         got = h_llr[j["llr_offset"]:j["llr_offset"] + oc.n_bp]
         np.testing.assert_array_equal(got.view(np.uint32), m[0].view(np.uint32))
         pk, _, it = oc.minsum_f32(m, 10, early_stop=True)
         np.testing.assert_array_equal(h_pk[j["out_offset"]:j["out_offset"] + oc.n_bytes], pk[0])
         assert h_it[i] == it[0]
+
+
+def test_modulation_order_validation(gpu):
+    b = Batch(max_jobs=4)
+    ok, *_ = make_jobs([1], 64, e=3000, qm=4)
+    b.set_jobs(ok)
+    for qm, e in ((3, 3000), (4, 3002), (12, 3000), (-2, 3000)):
+        bad, *_ = make_jobs([1], 64, e=e, qm=qm)
+        with pytest.raises(_lib.NrLdpcError):
+            b.set_jobs(bad)
 
 
 def test_mixed_batch_equals_per_code_decoders(gpu):
