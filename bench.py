@@ -185,9 +185,9 @@ def learned_vs_plain(dec, stream, batch: int, ebn0: float = 1.8, frames: int = 6
     weights (alpha 0.75) at the learned cap, and the flooding decoder with
     its own trained weights (weights/bg1_T10) at 10 iterations."""
     import torch
-    from nr_ldpc_gb300 import codes
-    from nr_ldpc_gb300.evaluate import clopper_pearson
-    from nr_ldpc_gb300.learned import load_weights
+    from nr_gpu_ldpc_gb300 import codes
+    from nr_gpu_ldpc_gb300.evaluate import clopper_pearson
+    from nr_gpu_ldpc_gb300.learned import load_weights
     sigma = codes.noise_sigma(ebn0, K_INFO / (N_BP - 2 * Z))
     sig = torch.full((batch,), sigma, dtype=torch.float32, device="cuda")
     out = torch.empty((batch, dec.packed_bytes), dtype=torch.uint8, device="cuda")
@@ -248,7 +248,7 @@ def mixed_batch(stream, n: int = 8192, n_iter: int = 10, reps: int = 5):
     one persistent CUDA-graph launch, early stop, at most n_iter iterations.
     Returns info Gbit/s (sum of K' over the batch / decode time) and FER."""
     import torch
-    from nr_ldpc_gb300.batch import Batch, make_jobs
+    from nr_gpu_ldpc_gb300.batch import Batch, make_jobs
     rng = np.random.default_rng(2024)
     bg = rng.integers(1, 3, n)
     z = rng.choice((64, 96, 128, 192, 256, 320, 384), n)
@@ -293,7 +293,7 @@ def training_step(steps: int = 5):
     BG2 Z=128, 8 unrolled iterations, 16,384 codewords per step (generation,
     forward, adjoint, Adam all on the GPU); milliseconds per step."""
     import torch
-    from nr_ldpc_gb300.learned import Trainer
+    from nr_gpu_ldpc_gb300.learned import Trainer
     tr = Trainer(bg=2, z=128, n_iter=8, batch=16384, chunk=4096, lr=1e-3, seed=5)
     for _ in range(2):
         tr.step()
@@ -321,8 +321,8 @@ def c1_fer_curve(dec, batch: int = 4096):
     Clopper-Pearson interval, early stop off; and the average iterations with
     early stop on."""
     import torch
-    from nr_ldpc_gb300 import codes
-    from nr_ldpc_gb300.evaluate import clopper_pearson
+    from nr_gpu_ldpc_gb300 import codes
+    from nr_gpu_ldpc_gb300.evaluate import clopper_pearson
     out = torch.empty((batch, dec.packed_bytes), dtype=torch.uint8, device="cuda")
     pts = []
     for k in range(9):
@@ -345,7 +345,7 @@ def c0_default_code(n: int = 640, n_iter: int = 5, reps: int = 20):
     point, and the batch decode time through the host-buffer call (copies
     included, as the README's timings are)."""
     import torch
-    from nr_ldpc_gb300 import Decoder, codes
+    from nr_gpu_ldpc_gb300 import Decoder, codes
     dec = Decoder(z=96, base=codes.wifi_base(), max_batch=n)
     k_info = dec.kb * dec.z
     pts = []
@@ -377,7 +377,7 @@ def c0_default_code(n: int = 640, n_iter: int = 5, reps: int = 20):
 def cpu_baseline(llr_host: np.ndarray, n_sample: int):
     """Reference algorithm on the host cores: the oracle's C restatement of
     the reference min-sum (kind 'port'), all cores, one codeword per thread."""
-    from nr_ldpc_gb300 import codes
+    from nr_gpu_ldpc_gb300 import codes
     from oracle.oracle import OracleCode
     oc = OracleCode(codes.base_matrix(BG, codes.set_index(Z)), Z)
     cores = os.cpu_count() or 1
@@ -411,7 +411,7 @@ def run_reference(args, world, rank):
     build for sm_103a / CUDA 13 as shipped)."""
     if rank != 0:
         return
-    from nr_ldpc_gb300 import codes
+    from nr_gpu_ldpc_gb300 import codes
     from oracle.oracle import OracleCode
     oc = OracleCode(codes.base_matrix(BG, codes.set_index(Z)), Z)
     cores = os.cpu_count() or 1
@@ -466,7 +466,7 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    from nr_ldpc_gb300 import Decoder, codes
+    from nr_gpu_ldpc_gb300 import Decoder, codes
 
     dec = Decoder(bg=BG, z=Z, max_batch=B, device=local)
     stream = torch.cuda.current_stream()

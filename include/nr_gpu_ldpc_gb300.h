@@ -1,5 +1,5 @@
 /*
- * nr_ldpc_gb300 -- GB300 (sm_103a) 5G NR / QC-LDPC normalized min-sum decoder.
+ * nr_gpu_ldpc_gb300 -- GB300 (sm_103a) 5G NR / QC-LDPC normalized min-sum decoder.
  *
  * C ABI: plain pointers and sizes, no C++ or framework types.  Every entry
  * point returns an nrldpc_status (0 = OK, negative = error) and never exits
@@ -28,8 +28,8 @@
  *            src/ldpc_kernels.cu:463-467,482-500, src/host_helpers.cpp:60-64.
  *            For Z % 8 == 0 this is byte-identical to the reference stream.
  */
-#ifndef NR_LDPC_GB300_H
-#define NR_LDPC_GB300_H
+#ifndef NR_GPU_LDPC_GB300_H
+#define NR_GPU_LDPC_GB300_H
 
 #include <stddef.h>
 #include <stdint.h>

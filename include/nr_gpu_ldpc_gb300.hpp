@@ -1,4 +1,4 @@
-// Header-only C++ convenience layer over the C ABI in nr_ldpc_gb300.h,
+// Header-only C++ convenience layer over the C ABI in nr_gpu_ldpc_gb300.h,
 // shaped after the reference's host calls (ctarver/NR_GPU_LDPC):
 //   setup_ldpc(A, rate, n_iterations)             src/nr_ldpc.h:14
 //   perform_gpu_ldpc_decoding<T>(d, h, g, I, s)   src/gpu_decoder_top.h:13-18
@@ -16,7 +16,7 @@
 #include <type_traits>
 #include <vector>
 
-#include "nr_ldpc_gb300.h"
+#include "nr_gpu_ldpc_gb300.h"
 
 namespace nrldpc {
 

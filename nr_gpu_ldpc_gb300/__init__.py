@@ -1,4 +1,4 @@
-"""nr_ldpc_gb300 -- GB300-native 5G NR / QC-LDPC min-sum decoding.
+"""nr_gpu_ldpc_gb300 -- GB300-native 5G NR / QC-LDPC min-sum decoding.
 
 * ``codes``    base graphs, lifting sizes, ``setup_ldpc`` (host logic, no GPU)
 * ``Decoder``  the GPU decoder over the C-ABI library ``libnrldpc_gb300.so``

@@ -2,7 +2,7 @@
 
 There is no fallback: if the library is missing or cannot be loaded, every
 GPU entry point raises.  Symbol list = the declarations of
-include/nr_ldpc_gb300.h.
+include/nr_gpu_ldpc_gb300.h.
 """
 from __future__ import annotations
 
@@ -90,7 +90,7 @@ def load(build_if_missing: bool = True):
         return _lib
     if not os.path.exists(LIB_PATH):
         if not build_if_missing:
-            raise NrLdpcError("load", -8, f"{LIB_PATH} missing; run nr_ldpc_gb300.build.build()")
+            raise NrLdpcError("load", -8, f"{LIB_PATH} missing; run nr_gpu_ldpc_gb300.build.build()")
         from . import build as _build
         _build.build()
     try:

@@ -8,7 +8,7 @@ the SM busier.  For each code this times the persistent batch decode of a
 homogeneous job list at every admissible value and keeps the fastest; the
 table is stored per GPU model and applied by ``Batch``/``Decoder``.
 
-    python -m nr_ldpc_gb300.autotune [--z 64 96 128 ...] [--iters 10] [--out PATH]
+    python -m nr_gpu_ldpc_gb300.autotune [--z 64 96 128 ...] [--iters 10] [--out PATH]
 """
 from __future__ import annotations
 

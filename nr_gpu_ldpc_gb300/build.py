@@ -41,7 +41,7 @@ def up_to_date() -> bool:
         return False
     t = os.path.getmtime(LIB)
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
-    deps.append(os.path.join(HERE, "..", "include", "nr_ldpc_gb300.h"))
+    deps.append(os.path.join(HERE, "..", "include", "nr_gpu_ldpc_gb300.h"))
     return all(os.path.getmtime(d) <= t for d in deps if os.path.exists(d))
 
 

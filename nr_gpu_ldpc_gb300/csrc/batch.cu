@@ -12,7 +12,7 @@
 #include <new>
 #include <vector>
 
-#include "../../include/nr_ldpc_gb300.h"
+#include "../../include/nr_gpu_ldpc_gb300.h"
 #include "channel_dev.cuh"
 #include "nrldpc_internal.h"
 

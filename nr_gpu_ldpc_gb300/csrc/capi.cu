@@ -1,4 +1,4 @@
-// C-ABI of the decoder (include/nr_ldpc_gb300.h): code setup, handles,
+// C-ABI of the decoder (include/nr_gpu_ldpc_gb300.h): code setup, handles,
 // device buffers and launches.  Host code only; kernels live in decode.cu
 // and channel.cu.
 #include <cuda_runtime.h>
@@ -10,7 +10,7 @@
 #include <new>
 #include <vector>
 
-#include "../../include/nr_ldpc_gb300.h"
+#include "../../include/nr_gpu_ldpc_gb300.h"
 #include "nrldpc_internal.h"
 
 using namespace nrldpc;

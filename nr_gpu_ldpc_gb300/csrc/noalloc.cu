@@ -29,7 +29,7 @@
 #include <algorithm>
 #include <mutex>
 
-#include "../../include/nr_ldpc_gb300.h"
+#include "../../include/nr_gpu_ldpc_gb300.h"
 #include "nrldpc_internal.h"
 
 namespace nrldpc {

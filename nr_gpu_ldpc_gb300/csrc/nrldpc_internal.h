@@ -5,7 +5,7 @@
 #include <cstddef>
 #include <cstdint>
 
-#include "../../include/nr_ldpc_gb300.h"
+#include "../../include/nr_gpu_ldpc_gb300.h"
 
 namespace nrldpc {
 

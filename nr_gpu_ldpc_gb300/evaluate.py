@@ -5,10 +5,10 @@ nrldpc_decode[_weighted], nrldpc_count_errors); only the four counters come
 back.  The reference counts errors over the info bits of each codeword
 (src/encoding_tools.cpp:112-155); so does this.
 
-    python -m nr_ldpc_gb300.evaluate --bg 1 --z 384 --ebn0 1.5 2.0 --iters 10 \
+    python -m nr_gpu_ldpc_gb300.evaluate --bg 1 --z 384 --ebn0 1.5 2.0 --iters 10 \
         [--weights bg1_T8] [--schedule layered] [--frames 100000] [--early-stop]
 
-    python -m nr_ldpc_gb300.evaluate --compare   # the learned-vs-plain table:
+    python -m nr_gpu_ldpc_gb300.evaluate --compare   # the learned-vs-plain table:
         BG1 Z=384, batch 16384, Eb/N0 1.0..2.0 dB, early stop on: plain
         flooding min-sum at 10 iterations, the learned layered decoder
         (weights/bg1_L6) at 4, 5, 6 iterations, the layered decoder without

@@ -1,7 +1,7 @@
 """Train learned weighted min-sum weights on the GPU and save them.
 
-    python -m nr_ldpc_gb300.train --bg 2 --z 128 --iters 8 --batch 16384 \
-        --steps 400 --lr 1e-3 --out nr_ldpc_gb300/weights/bg2_T8
+    python -m nr_gpu_ldpc_gb300.train --bg 2 --z 128 --iters 8 --batch 16384 \
+        --steps 400 --lr 1e-3 --out nr_gpu_ldpc_gb300/weights/bg2_T8
 
 Defaults follow the training configuration the project is specified on:
 8 unrolled iterations, weights initialised to 0.75, 16384 seeded codewords

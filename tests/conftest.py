@@ -24,7 +24,7 @@ def golden():
 def cuda_lib():
     """The in-tree CUDA library, built if missing (CPU-only host functions
     work without a GPU)."""
-    from nr_ldpc_gb300 import _lib
+    from nr_gpu_ldpc_gb300 import _lib
     return _lib.load(build_if_missing=True)
 
 

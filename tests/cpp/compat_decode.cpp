@@ -10,7 +10,7 @@
 #include <cstring>
 #include <vector>
 
-#include "nr_ldpc_gb300.hpp"
+#include "nr_gpu_ldpc_gb300.hpp"
 
 template <typename T>
 struct HostBuffers {  // the host_mem members the decode call reads

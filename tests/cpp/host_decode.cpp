@@ -1,4 +1,4 @@
-// A reference-style C++ caller of the decoder through include/nr_ldpc_gb300.hpp,
+// A reference-style C++ caller of the decoder through include/nr_gpu_ldpc_gb300.hpp,
 // shaped like the reference's test_throughput (src/main.cpp:147-171):
 // setup_ldpc -> one Decoder per stream -> perform_gpu_ldpc_decoding on pinned
 // host buffers -> synchronize.
@@ -12,7 +12,7 @@
 #include <cstdlib>
 #include <vector>
 
-#include "nr_ldpc_gb300.hpp"
+#include "nr_gpu_ldpc_gb300.hpp"
 
 int main(int argc, char** argv) {
     if (argc != 5 && argc != 6) {

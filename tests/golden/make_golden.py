@@ -27,7 +27,7 @@ import numpy as np
 
 ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), "..", ".."))
 sys.path.insert(0, ROOT)
-from nr_ldpc_gb300 import codes  # noqa: E402
+from nr_gpu_ldpc_gb300 import codes  # noqa: E402
 from oracle.oracle import OracleCode, RefEmu, build  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))

@@ -4,7 +4,7 @@ import ctypes as C
 import os
 import re
 
-from nr_ldpc_gb300 import _lib, codes
+from nr_gpu_ldpc_gb300 import _lib, codes
 
 HEADER_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "include")
 

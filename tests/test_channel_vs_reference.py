@@ -7,8 +7,8 @@ where oracle/_ref was not built)."""
 import numpy as np
 import pytest
 
-from nr_ldpc_gb300 import codes
-from nr_ldpc_gb300.evaluate import clopper_pearson
+from nr_gpu_ldpc_gb300 import codes
+from nr_gpu_ldpc_gb300.evaluate import clopper_pearson
 from oracle.oracle import OracleCode, RefEmu
 
 

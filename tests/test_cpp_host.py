@@ -1,4 +1,4 @@
-"""The C++ layer (include/nr_ldpc_gb300.hpp) from a reference-style host
+"""The C++ layer (include/nr_gpu_ldpc_gb300.hpp) from a reference-style host
 program: it compiles and links against the in-tree library with plain g++
 (CPU), and its decode equals the oracle's (GPU)."""
 import os
@@ -8,7 +8,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from nr_ldpc_gb300 import codes
+from nr_gpu_ldpc_gb300 import codes
 from oracle.oracle import OracleCode
 
 ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
@@ -19,8 +19,8 @@ def _build(tmp_path, cuda_lib, name="host_decode", std="c++17"):
     exe = str(tmp_path / name)
     cmd = ["g++", f"-std={std}", "-O2", os.path.join(ROOT, "tests", "cpp", name + ".cpp"), "-o", exe,
            "-I", os.path.join(ROOT, "include"), "-I", os.path.join(CUDA, "include"),
-           "-L", os.path.join(ROOT, "nr_ldpc_gb300"), "-lnrldpc_gb300",
-           "-Wl,-rpath," + os.path.join(ROOT, "nr_ldpc_gb300"),
+           "-L", os.path.join(ROOT, "nr_gpu_ldpc_gb300"), "-lnrldpc_gb300",
+           "-Wl,-rpath," + os.path.join(ROOT, "nr_gpu_ldpc_gb300"),
            "-L", os.path.join(CUDA, "lib64"), "-lcudart", "-Wl,-rpath," + os.path.join(CUDA, "lib64")]
     subprocess.run(cmd, check=True, capture_output=True, text=True)
     return exe

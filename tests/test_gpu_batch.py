@@ -5,8 +5,8 @@ import numpy as np
 import pytest
 import torch
 
-from nr_ldpc_gb300 import Decoder, _lib, codes
-from nr_ldpc_gb300.batch import Batch, make_jobs
+from nr_gpu_ldpc_gb300 import Decoder, _lib, codes
+from nr_gpu_ldpc_gb300.batch import Batch, make_jobs
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -161,7 +161,7 @@ def test_uneven_8192_codeword_mix(gpu):
 
 def test_crc_kernel_matches_oracle(gpu):
     import ctypes as C
-    from nr_ldpc_gb300 import _lib
+    from nr_gpu_ldpc_gb300 import _lib
     lib = _lib.load()
     rng = np.random.default_rng(1)
     for ctype, poly in enumerate((O.CRC24A, O.CRC24B, O.CRC16)):

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 import torch
 
-from nr_ldpc_gb300 import Decoder, _lib, codes
+from nr_gpu_ldpc_gb300 import Decoder, _lib, codes
 from oracle.oracle import OracleCode
 
 pytestmark = pytest.mark.gpu

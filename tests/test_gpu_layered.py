@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 import torch
 
-from nr_ldpc_gb300 import Decoder, codes
+from nr_gpu_ldpc_gb300 import Decoder, codes
 from oracle.oracle import OracleCode
 
 pytestmark = pytest.mark.gpu

@@ -4,8 +4,8 @@ import numpy as np
 import pytest
 import torch
 
-from nr_ldpc_gb300 import Decoder, codes
-from nr_ldpc_gb300.learned import Trainer
+from nr_gpu_ldpc_gb300 import Decoder, codes
+from nr_gpu_ldpc_gb300.learned import Trainer
 from oracle.oracle import OracleCode
 
 pytestmark = pytest.mark.gpu
@@ -104,8 +104,8 @@ def test_adam_step_matches_numpy(gpu):
     g = rng.normal(size=tr.w.shape)
     tr.grad.copy_(torch.from_numpy(g))
     w0 = tr.w.cpu().numpy().copy()
-    from nr_ldpc_gb300 import _lib
-    from nr_ldpc_gb300.decoder import _dev_ptr, _stream_ptr
+    from nr_gpu_ldpc_gb300 import _lib
+    from nr_gpu_ldpc_gb300.decoder import _dev_ptr, _stream_ptr
     lib = _lib.load()
     for step in (1, 2):
         assert lib.nrldpc_adam_step(tr.w.numel(), _dev_ptr(tr.w), _dev_ptr(tr.grad), _dev_ptr(tr.m),
@@ -170,7 +170,7 @@ def test_layered_short_training_lowers_the_loss(gpu):
 
 
 def test_weight_rows_limit(gpu):
-    from nr_ldpc_gb300 import _lib
+    from nr_gpu_ldpc_gb300 import _lib
     dec = Decoder(bg=2, z=16, max_batch=4)
     with pytest.raises(_lib.NrLdpcError):
         dec.set_weights(np.full((17, dec.n_edges), 0.75, np.float32))
@@ -182,7 +182,7 @@ def test_trained_weights_gain_over_plain(gpu):
     1.8 dB, 16384 seeded codewords, early stop): the learned layered decoder
     at <= 6 iterations has a lower FER than the same layered decoder with the
     plain alpha = 0.75 and than plain flooding min-sum at 10 iterations."""
-    from nr_ldpc_gb300.learned import load_weights
+    from nr_gpu_ldpc_gb300.learned import load_weights
     n = 8192
     dec = Decoder(bg=1, z=384, max_batch=n)
     sig = torch.full((n,), codes.noise_sigma(1.8, 22 / 66), device=gpu)

@@ -2,7 +2,7 @@
 without a reference counterpart (the reference decodes flooding only)."""
 import numpy as np
 
-from nr_ldpc_gb300 import codes
+from nr_gpu_ldpc_gb300 import codes
 from oracle.oracle import OracleCode
 
 

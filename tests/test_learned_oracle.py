@@ -4,7 +4,7 @@ min/sign structure away from ties, so central differences are exact up to
 the smooth softplus terms."""
 import numpy as np
 
-from nr_ldpc_gb300 import codes
+from nr_gpu_ldpc_gb300 import codes
 from oracle.oracle import OracleCode
 
 

@@ -7,7 +7,7 @@ import os
 import numpy as np
 import pytest
 
-from nr_ldpc_gb300 import codes
+from nr_gpu_ldpc_gb300 import codes
 from oracle.oracle import OracleCode
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 

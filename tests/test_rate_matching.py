@@ -5,7 +5,7 @@ LLRs."""
 import numpy as np
 import pytest
 
-from nr_ldpc_gb300 import codes
+from nr_gpu_ldpc_gb300 import codes
 from oracle import oracle as O
 
 

@@ -7,7 +7,7 @@ import torch
 import torch.distributed as dist
 import torch.multiprocessing as mp
 
-from nr_ldpc_gb300.replicas import max_over_ranks, reduce_counts, shard
+from nr_gpu_ldpc_gb300.replicas import max_over_ranks, reduce_counts, shard
 
 
 def test_shard_covers_batch_exactly():

@@ -6,7 +6,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from nr_ldpc_gb300 import _lib
+from nr_gpu_ldpc_gb300 import _lib
 from oracle import oracle as O
 
 
@@ -46,7 +46,7 @@ def test_segment_known_cases(cuda_lib):
 @pytest.mark.parametrize("B,bg", [(16848, 1), (8448, 1), (12096, 2), (100000 - 100000 % 8 + 8, 1)])
 def test_gpu_segment_desegment_round_trip(gpu, B, bg):
     import torch
-    from nr_ldpc_gb300 import segmentation as S
+    from nr_gpu_ldpc_gb300 import segmentation as S
     info = O.segment_info(B, bg)
     if info is None:
         pytest.skip("not a segmentable size")

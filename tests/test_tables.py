@@ -4,7 +4,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from nr_ldpc_gb300 import codes
+from nr_gpu_ldpc_gb300 import codes
 from oracle.oracle import OracleCode
 
 

@@ -14,7 +14,7 @@ import ctypes as C
 import pytest
 import torch
 
-from nr_ldpc_gb300 import Decoder, _lib, codes
+from nr_gpu_ldpc_gb300 import Decoder, _lib, codes
 
 pytestmark = pytest.mark.gpu
 
