@@ -59,7 +59,11 @@ int main(int argc, char** argv) {
             HostBuffers<float> h{llr, counts[s] * p.N_before_puncture * 4, out, counts[s] * packed};
             nrldpc::compat::perform_gpu_ldpc_decoding(&d, &h, &g, p.n_iterations, s);
         }
-        cudaDeviceSynchronize();
+        const cudaError_t err = cudaDeviceSynchronize();
+        if (err != cudaSuccess) {
+            std::fprintf(stderr, "decode failed on the GPU: %s\n", cudaGetErrorString(err));
+            return 6;
+        }
         FILE* o = std::fopen(argv[2], "wb");
         if (!o) return 5;
         for (int s = 0; s < n_streams; s++) std::fwrite(out[s], 1, static_cast<size_t>(counts[s]) * packed, o);

@@ -39,7 +39,11 @@ int main(int argc, char** argv) {
         cudaStream_t stream;
         cudaStreamCreate(&stream);
         dec.perform_gpu_ldpc_decoding(llr, packed, n_cw, p.n_iterations, stream);
-        cudaStreamSynchronize(stream);
+        const cudaError_t err = cudaStreamSynchronize(stream);
+        if (err != cudaSuccess) {
+            std::fprintf(stderr, "decode failed on the GPU: %s\n", cudaGetErrorString(err));
+            return 6;
+        }
         FILE* g = std::fopen(argv[4], "wb");
         if (!g) return 5;
         std::fwrite(packed, 1, static_cast<size_t>(n_cw) * dec.packed_bytes(), g);
