@@ -133,8 +133,8 @@ int nrldpc_decode_host_async_q(nrldpc_handle* h, const void* h_llr_q, int qtype,
  *   HOST_AUTO    (default) DIRECT when both buffers are pinned, the GPU
  *                reaches host memory over a coherent link (Grace CPU with
  *                NVLink-C2C: cudaDevAttrPageableMemoryAccessUsesHostPageTables)
- *                and the batch is at most 8 rounds of the decoder's resident
- *                CTAs (2432 BG1 Z=384 codewords on a GB300); otherwise COPY. */
+ *                and the batch is at most 4 rounds of the decoder's resident
+ *                CTAs (1216 BG1 Z=384 codewords on a GB300); otherwise COPY. */
 enum { NRLDPC_HOST_AUTO = 0, NRLDPC_HOST_COPY = 1, NRLDPC_HOST_DIRECT = 2 };
 int nrldpc_set_host_transfer(nrldpc_handle* h, int mode);
 

@@ -20,11 +20,13 @@ namespace {
 
 const int kBaseZ[8] = {2, 3, 5, 7, 9, 11, 13, 15};
 constexpr int kHostChunks = 16;  // most chunks of one host-buffer decode
+constexpr int kChunkCounter = 4;  // first scratch word of the per-chunk work counters
+constexpr size_t kScratchBytes = 128;
 // Largest batch, in CTA rounds, that NRLDPC_HOST_AUTO decodes straight from
-// host memory (GB300, BG1 Z=384, 10 iterations: direct ahead of staged copies
-// by 10% at 1 round and 8% at 4, 1% behind to 2% ahead at 13.5 depending on
-// the run, 1% behind at 27).
-constexpr size_t kDirectMaxRounds = 8;
+// host memory (GB300, BG1 Z=384, 10 iterations, against the two-lane staged
+// pipeline: direct ahead by 9% at half a round and 10% at 1, 3% at 4; behind
+// by 3% at 6, 1% at 8, 5% at 10 and 2% at 13.5).
+constexpr size_t kDirectMaxRounds = 4;
 
 struct Handle {
     int device = 0;
@@ -36,7 +38,10 @@ struct Handle {
     int cpb = 1, threads = 32, ctas_per_sm = 1, sm_count = 1, max_grid = 1, minb = 1;
     size_t smem = 0;
     uint32_t* state = nullptr;
-    int* scratch = nullptr;  // [0] work counter, [1] error flag
+    uint32_t* state2 = nullptr;  // the second lane's check-node state (host-buffer pipeline)
+    // [0] work counter, [1] error flag, [kChunkCounter + k] work counter of
+    // chunk k of a host-buffer decode
+    int* scratch = nullptr;
     float* stage_llr = nullptr;
     uint8_t* stage_packed = nullptr;
     void* stage_q = nullptr;  // fp16 / int8 LLR staging (nrldpc_decode_host_async_q)
@@ -46,9 +51,14 @@ struct Handle {
     int schedule = NRLDPC_SCHEDULE_FLOODING;
     int host_mode = NRLDPC_HOST_AUTO;
     bool coherent_host = false;  // the GPU reads host memory over a coherent link (Grace C2C)
-    // host-buffer pipeline: copies of chunk k+1 overlap the decode of chunk k
+    // host-buffer pipeline: copies of chunk k+1 overlap the decode of chunk
+    // k; chunks alternate between two lanes (the caller's stream and
+    // lane_stream, each with its own check-node state), so a chunk's decode
+    // starts while the previous one drains
     cudaStream_t copy_stream = nullptr;
+    cudaStream_t lane_stream = nullptr;
     cudaEvent_t ev_start = nullptr;
+    cudaEvent_t ev_lane = nullptr;
     cudaEvent_t ev_chunk[kHostChunks] = {};
 };
 
@@ -140,6 +150,7 @@ int base_matrix_impl(int bg, int ils, int* out, int* rows, int* cols) {
 void free_handle(Handle* h) {
     if (!h) return;
     cudaFree(h->state);
+    cudaFree(h->state2);
     cudaFree(h->scratch);
     cudaFree(h->stage_llr);
     cudaFree(h->stage_packed);
@@ -148,7 +159,9 @@ void free_handle(Handle* h) {
     for (cudaEvent_t e : h->ev_chunk)
         if (e) cudaEventDestroy(e);
     if (h->ev_start) cudaEventDestroy(h->ev_start);
+    if (h->ev_lane) cudaEventDestroy(h->ev_lane);
     if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
+    if (h->lane_stream) cudaStreamDestroy(h->lane_stream);
     delete h;
 }
 
@@ -213,10 +226,14 @@ int init_impl(const int* base, int rows, int cols, int kb, const nrldpc_config* 
         static_cast<size_t>(h->max_grid) * cpb * h->tab.rows * static_cast<size_t>(z);
     const size_t n_llr = static_cast<size_t>(cfg->max_batch) * h->tab.n_bp;
     if (cudaMalloc(&h->state, state_elems * kStateBytesPerRow) != cudaSuccess ||
-        cudaMalloc(&h->scratch, 64) != cudaSuccess || cudaMemset(h->scratch, 0, 64) != cudaSuccess ||
+        cudaMalloc(&h->state2, state_elems * kStateBytesPerRow) != cudaSuccess ||
+        cudaMalloc(&h->scratch, kScratchBytes) != cudaSuccess ||
+        cudaMemset(h->scratch, 0, kScratchBytes) != cudaSuccess ||
         cudaMalloc(&h->stage_llr, n_llr * sizeof(float)) != cudaSuccess ||
         cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->lane_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->ev_start, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_lane, cudaEventDisableTiming) != cudaSuccess ||
         cudaMalloc(&h->stage_packed,
                    static_cast<size_t>(cfg->max_batch) * h->tab.packed_bytes) != cudaSuccess) {
         free_handle(h);
@@ -232,9 +249,12 @@ int init_impl(const int* base, int rows, int cols, int kb, const nrldpc_config* 
 }
 
 // llr_from_host: llr is the device view of pinned host memory; the kernel
-// reads it with ordinary loads instead of bulk copies.
+// reads it with ordinary loads instead of bulk copies.  counter / state: a
+// work counter that is already zero and a check-node state of the host-buffer
+// pipeline's lanes (null: the handle's own, the counter cleared here).
 int decode_impl(Handle* h, const float* llr, uint8_t* packed, int n_cw, int n_iter, int early,
-                float* app, int32_t* iters, bool weighted, cudaStream_t stream, bool llr_from_host = false) {
+                float* app, int32_t* iters, bool weighted, cudaStream_t stream, bool llr_from_host = false,
+                int* counter = nullptr, uint32_t* state = nullptr) {
     if (!h || n_cw < 0 || n_iter < 1 || (early != 0 && early != 1)) return NRLDPC_ERR_INVALID_ARG;
     if (n_cw == 0) return NRLDPC_OK;  // empty batch: nothing to read or write
     if (!llr || !packed) return NRLDPC_ERR_INVALID_ARG;
@@ -246,8 +266,8 @@ int decode_impl(Handle* h, const float* llr, uint8_t* packed, int n_cw, int n_it
     a.packed = packed;
     a.app = app;
     a.iters = iters;
-    a.state = h->state;
-    a.work_counter = h->scratch;
+    a.state = state ? state : h->state;
+    a.work_counter = counter ? counter : h->scratch;
     a.error_flag = h->scratch + 1;
     a.n_cw = n_cw;
     a.n_iter = n_iter;
@@ -258,8 +278,7 @@ int decode_impl(Handle* h, const float* llr, uint8_t* packed, int n_cw, int n_it
     a.alpha = h->alpha;
     a.llr_from_host = llr_from_host ? 1 : 0;
     const int grid = std::min(a.n_groups, h->max_grid);
-    cudaError_t e = cudaMemsetAsync(h->scratch, 0, sizeof(int), stream);
-    if (e != cudaSuccess) return NRLDPC_ERR_CUDA;
+    if (!counter && cudaMemsetAsync(h->scratch, 0, sizeof(int), stream) != cudaSuccess) return NRLDPC_ERR_CUDA;
     return map_cuda(launch_decode(h->tab, a, weighted ? h->weights : nullptr, grid, h->threads, h->smem,
                                   h->schedule == NRLDPC_SCHEDULE_LAYERED, h->minb, stream));
 }
@@ -267,8 +286,11 @@ int decode_impl(Handle* h, const float* llr, uint8_t* packed, int n_cw, int n_it
 // Host-buffer decode (fp32 LLRs, or narrow ones widened on the GPU: qtype 1
 // fp16, 2 int8 * scale).  The batch is cut into chunks of whole CTA rounds
 // (1, 2, 4, ... rounds of max_grid * cpb codewords): chunk k+1's host->device
-// copy runs on the handle's copy stream while chunk k decodes on the caller's
-// stream, and each chunk's packed bits go back as soon as it is decoded.
+// copy runs on the handle's copy stream while chunk k decodes, and each
+// chunk's packed bits go back as soon as it is decoded.  Even chunks decode
+// on the caller's stream, odd ones on the handle's lane stream with their own
+// check-node state and work counter, so the next chunk's CTAs take over SMs
+// as the current chunk's CTAs finish instead of after the whole launch.
 // Device view of a pinned (cudaHostAlloc'd or registered) host buffer, or
 // null when the GPU cannot address it.
 void* pinned_device_view(const void* p) {
@@ -301,35 +323,52 @@ int host_decode(Handle* h, const void* h_llr, int qtype, float scale, uint8_t* h
     const size_t n_bp = static_cast<size_t>(h->tab.n_bp);
     const size_t in_elem = qtype == 0 ? 4 : (qtype == 1 ? 2 : 1);
     void* stage_in = qtype == 0 ? static_cast<void*>(h->stage_llr) : h->stage_q;
-    // the copy stream must not overwrite staging a previous call still reads
-    if (cudaEventRecord(h->ev_start, s) != cudaSuccess ||
-        cudaStreamWaitEvent(h->copy_stream, h->ev_start, 0) != cudaSuccess)
+    // per-chunk work counters zeroed at once; the copy stream must not
+    // overwrite staging a previous call still reads, and the second lane
+    // starts after the caller's earlier work
+    if (cudaMemsetAsync(h->scratch + kChunkCounter, 0, kHostChunks * sizeof(int), s) != cudaSuccess ||
+        cudaEventRecord(h->ev_start, s) != cudaSuccess ||
+        cudaStreamWaitEvent(h->copy_stream, h->ev_start, 0) != cudaSuccess ||
+        cudaStreamWaitEvent(h->lane_stream, h->ev_start, 0) != cudaSuccess)
         return NRLDPC_ERR_CUDA;
+    int rc = NRLDPC_OK;
     size_t begin = 0;
     size_t rounds = 1;
     for (int k = 0; begin < static_cast<size_t>(n_cw); k++) {
         size_t count = std::min(static_cast<size_t>(n_cw) - begin, rounds * round);
         if (k == kHostChunks - 1) count = static_cast<size_t>(n_cw) - begin;  // last event: the rest
         rounds *= 2;  // each copy hides behind the decode of a chunk half its size
+        cudaStream_t ls = (k & 1) ? h->lane_stream : s;
         const char* src = static_cast<const char*>(h_llr) + begin * n_bp * in_elem;
         char* dst = static_cast<char*>(stage_in) + begin * n_bp * in_elem;
         if (cudaMemcpyAsync(dst, src, count * n_bp * in_elem, cudaMemcpyHostToDevice, h->copy_stream) !=
                 cudaSuccess ||
             cudaEventRecord(h->ev_chunk[k], h->copy_stream) != cudaSuccess ||
-            cudaStreamWaitEvent(s, h->ev_chunk[k], 0) != cudaSuccess)
-            return NRLDPC_ERR_CUDA;
+            cudaStreamWaitEvent(ls, h->ev_chunk[k], 0) != cudaSuccess) {
+            rc = NRLDPC_ERR_CUDA;
+            break;
+        }
         float* llr = h->stage_llr + begin * n_bp;
-        if (qtype != 0 && launch_dequant(dst, qtype, scale, count * n_bp, llr, s) != cudaSuccess)
-            return NRLDPC_ERR_CUDA;
+        if (qtype != 0 && launch_dequant(dst, qtype, scale, count * n_bp, llr, ls) != cudaSuccess) {
+            rc = NRLDPC_ERR_CUDA;
+            break;
+        }
         uint8_t* out = h->stage_packed + begin * h->tab.packed_bytes;
-        const int rc = decode_impl(h, llr, out, static_cast<int>(count), n_iter, early, nullptr, nullptr, false, s);
-        if (rc) return rc;
+        rc = decode_impl(h, llr, out, static_cast<int>(count), n_iter, early, nullptr, nullptr, false, ls, false,
+                         h->scratch + kChunkCounter + k, (k & 1) ? h->state2 : h->state);
+        if (rc) break;
         if (cudaMemcpyAsync(h_packed + begin * h->tab.packed_bytes, out, count * h->tab.packed_bytes,
-                            cudaMemcpyDeviceToHost, s) != cudaSuccess)
-            return NRLDPC_ERR_CUDA;
+                            cudaMemcpyDeviceToHost, ls) != cudaSuccess) {
+            rc = NRLDPC_ERR_CUDA;
+            break;
+        }
         begin += count;
     }
-    return NRLDPC_OK;
+    // the caller's stream covers the second lane's work too
+    if (cudaEventRecord(h->ev_lane, h->lane_stream) != cudaSuccess ||
+        cudaStreamWaitEvent(s, h->ev_lane, 0) != cudaSuccess)
+        return NRLDPC_ERR_CUDA;
+    return rc;
 }
 
 }  // namespace

@@ -138,7 +138,7 @@ class Decoder:
         """How decode_host moves fp32 data: 'copy' (staged chunk copies),
         'direct' (the decoder reads the LLRs from pinned host memory and
         writes the bits back itself) or 'auto' (default: 'direct' for pinned
-        buffers on a GPU with a coherent host link up to 8 rounds of
+        buffers on a GPU with a coherent host link up to 4 rounds of
         resident CTAs, else 'copy')."""
         code = {"auto": 0, "copy": 1, "direct": 2}.get(mode, mode)
         _lib.check("nrldpc_set_host_transfer", self._lib.nrldpc_set_host_transfer(self._h, int(code)))
