@@ -107,8 +107,10 @@ int nrldpc_decode(nrldpc_handle* h, const float* d_llr, uint8_t* d_packed, int n
 /* Host buffers (pinned for overlap, pageable works): H2D into the handle's
  * staging, decode, D2H -- queued on `stream`, returns without waiting.  The
  * batch moves in chunks: the host->device copy of chunk k+1 runs on the
- * handle's own copy stream while chunk k decodes on `stream`; all of it is
- * ordered after earlier work on `stream` and done when `stream` is.  Pinned
+ * handle's own copy stream while chunk k decodes, even chunks on `stream`
+ * and odd ones on a second stream the handle owns (with its own check-node
+ * scratch); all of it is ordered after earlier work on `stream` and done
+ * when `stream` is.  Pinned
  * buffers may instead be read and written by the decoder itself over the
  * host link (nrldpc_set_host_transfer, below). */
 int nrldpc_decode_host_async(nrldpc_handle* h, const float* h_llr, uint8_t* h_packed, int n_cw,
