@@ -295,6 +295,17 @@ int nrldpc_cb_desegment(const uint8_t* d_blocks, int block_stride, const nrldpc_
 /* Last device-side error recorded by a bounded wait (0 if none); clears it. */
 int nrldpc_device_error(nrldpc_handle* h);
 
+/* Self-test of the bounded device-side wait (no reference counterpart): one
+ * device-resident decode of n_cw codewords whose copy barrier is told to
+ * expect 16 bytes more than the LLR copies deliver, with a short wait limit.
+ * Every CTA's wait for its first codeword runs out, the kernel records the
+ * timeout (nrldpc_device_error then returns NRLDPC_ERR_TIMEOUT) and its CTAs
+ * return without writing d_packed.  Nothing faults or spins without end: the
+ * copies land, only the barrier's phase never completes.  The handle stays
+ * usable. */
+int nrldpc_selftest_wait_timeout(nrldpc_handle* h, const float* d_llr, uint8_t* d_packed, int n_cw,
+                                 nrldpc_stream_t stream);
+
 const char* nrldpc_status_string(int status);
 
 #ifdef __cplusplus

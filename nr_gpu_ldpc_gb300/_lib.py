@@ -79,6 +79,7 @@ SIGNATURES = {
     "nrldpc_cb_desegment": (_i, [_vp, _i, C.POINTER(SegmentInfoC), _vp, _vp, _vp]),
     "nrldpc_decode_noalloc": (_i, [_i, _i, _f, _vp, _vp, _i, _i, _i, _vp]),
     "nrldpc_device_error": (_i, [_vp]),
+    "nrldpc_selftest_wait_timeout": (_i, [_vp, _vp, _vp, _i, _vp]),
     "nrldpc_status_string": (C.c_char_p, [_i]),
 }
 

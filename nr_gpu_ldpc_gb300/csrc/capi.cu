@@ -254,7 +254,7 @@ int init_impl(const int* base, int rows, int cols, int kb, const nrldpc_config* 
 // pipeline's lanes (null: the handle's own, the counter cleared here).
 int decode_impl(Handle* h, const float* llr, uint8_t* packed, int n_cw, int n_iter, int early,
                 float* app, int32_t* iters, bool weighted, cudaStream_t stream, bool llr_from_host = false,
-                int* counter = nullptr, uint32_t* state = nullptr) {
+                int* counter = nullptr, uint32_t* state = nullptr, int wait_limit = 0, uint32_t extra_tx = 0) {
     if (!h || n_cw < 0 || n_iter < 1 || (early != 0 && early != 1)) return NRLDPC_ERR_INVALID_ARG;
     if (n_cw == 0) return NRLDPC_OK;  // empty batch: nothing to read or write
     if (!llr || !packed) return NRLDPC_ERR_INVALID_ARG;
@@ -277,6 +277,8 @@ int decode_impl(Handle* h, const float* llr, uint8_t* packed, int n_cw, int n_it
     a.early_stop = early;
     a.alpha = h->alpha;
     a.llr_from_host = llr_from_host ? 1 : 0;
+    a.wait_limit = wait_limit;
+    a.extra_tx = extra_tx;
     const int grid = std::min(a.n_groups, h->max_grid);
     if (!counter && cudaMemsetAsync(h->scratch, 0, sizeof(int), stream) != cudaSuccess) return NRLDPC_ERR_CUDA;
     return map_cuda(launch_decode(h->tab, a, weighted ? h->weights : nullptr, grid, h->threads, h->smem,
@@ -508,6 +510,13 @@ int nrldpc_decode(nrldpc_handle* handle, const float* d_llr, uint8_t* d_packed, 
                   nrldpc_stream_t stream) {
     return decode_impl(reinterpret_cast<Handle*>(handle), d_llr, d_packed, n_cw, n_iter, early_stop,
                        d_app, d_iters, false, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int nrldpc_selftest_wait_timeout(nrldpc_handle* handle, const float* d_llr, uint8_t* d_packed, int n_cw,
+                                 nrldpc_stream_t stream) {
+    // 16 bytes more than the copies deliver, 1024 wait iterations
+    return decode_impl(reinterpret_cast<Handle*>(handle), d_llr, d_packed, n_cw, 1, 0, nullptr, nullptr, false,
+                       reinterpret_cast<cudaStream_t>(stream), false, nullptr, nullptr, 1024, 16);
 }
 
 int nrldpc_decode_weighted(nrldpc_handle* handle, const float* d_llr, uint8_t* d_packed, int n_cw,

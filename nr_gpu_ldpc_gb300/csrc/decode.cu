@@ -84,8 +84,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
 }
 
 // Bounded wait: false when the limit ran out (the caller records an error).
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
-    for (long i = 0; i < kWaitLimit; i++)
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, long limit = kWaitLimit) {
+    for (long i = 0; i < limit; i++)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -533,15 +533,16 @@ __global__ void __launch_bounds__(kMaxThreads, MINB)
         } else {
             if (tid == 0) {  // core-column LLRs of each codeword into its Lold
                 fence_proxy_async();
-                mbar_arrive_expect_tx(bar, static_cast<uint32_t>(n_valid) * cf * 4u);
+                mbar_arrive_expect_tx(bar, static_cast<uint32_t>(n_valid) * cf * 4u + a.extra_tx);
                 for (int k = 0; k < n_valid; k++)
                     bulk_g2s(smem_addr(buf0 + static_cast<size_t>(k) * cf),
                              a.llr + static_cast<size_t>(cw0 + k) * n, cf * 4u, bar);
             }
-            bool ok = mbar_wait_bounded(bar, phase);
+            const long limit = a.wait_limit > 0 ? a.wait_limit : kWaitLimit;
+            bool ok = mbar_wait_bounded(bar, phase, limit);
             if (!__syncthreads_and(ok)) {
                 if (tid == 0) atomicExch(a.error_flag, kErrLlrLoadTimeout);
-                mbar_wait_bounded(bar, phase);  // let the copy in flight land before leaving
+                mbar_wait_bounded(bar, phase, limit);  // let the copy in flight land before leaving
                 return;
             }
             phase ^= 1u;

@@ -76,6 +76,11 @@ struct DecodeArgs {
     int n_cw, n_iter, cpb, n_groups, n_w_iters, early_stop;
     int llr_from_host;      // 1: llr is pinned host memory read over the host link
     float alpha;
+    // bounded-wait self-test only (0 in every decode): iterations of the LLR
+    // copy wait (0: the default limit), and bytes the copy barrier expects
+    // beyond what the copies deliver, so that wait runs out
+    int wait_limit;
+    uint32_t extra_tx;
 };
 
 enum DeviceError : int { kErrNone = 0, kErrLlrLoadTimeout = 1 };

@@ -324,3 +324,30 @@ def test_every_lifting_size_against_oracle(gpu, bg):
         opl, _, _ = oc.layered_f32(llr, 3, threads=3)
         np.testing.assert_array_equal(pl.cpu().numpy(), opl, err_msg=f"layered bg{bg} z{z}")
         dec.close()
+
+
+def test_bounded_wait_reports_timeout(gpu):
+    """The wait for a group's LLR copy is bounded.  The self-test entry point
+    tells the copy barrier to expect 16 bytes more than the copies deliver,
+    so no CTA's wait can complete: each gives up after its limit, the kernel
+    records the timeout and returns, the host reads it (and reading clears
+    it), and the same handle then decodes bit-exactly again."""
+    lib = _lib.load()
+    z, n = 384, 8
+    oc = OracleCode(codes.base_matrix(1, codes.set_index(z)), z)
+    llr, _ = oc.gen_llr(22, 77, 0, np.full(n, codes.noise_sigma(2.0, 1 / 3), np.float32), 2)
+    dec = make_decoder(1, z, max_batch=n)
+    d_llr = torch.from_numpy(llr).to(gpu)
+    out = torch.zeros((n, dec.packed_bytes), dtype=torch.uint8, device=gpu)
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert lib.nrldpc_selftest_wait_timeout(dec._h, C.c_void_p(d_llr.data_ptr()), C.c_void_p(out.data_ptr()),
+                                            n, stream) == 0
+    torch.cuda.synchronize()
+    assert dec.device_error() == -6  # NRLDPC_ERR_TIMEOUT: the LLR-load wait ran out
+    assert dec.device_error() == 0
+    packed = dec.decode(d_llr, 5)
+    torch.cuda.synchronize()
+    want, _, _ = oc.minsum_f32(llr, 5)
+    assert np.array_equal(packed.cpu().numpy(), want)
+    assert dec.device_error() == 0
+    dec.close()
