@@ -12,7 +12,8 @@ the same metric through the reference-shaped host call
 ``learned_vs_plain`` (in the same line) compares the learned decoder with plain
 min-sum at a stated Eb/N0 where plain flooding at 10 iterations has FER <=
 1e-2: FER with 95% intervals over 65,536 fresh codewords and info Gbit/s of
-each (early stop on for both).  ``mixed_batch`` times the uneven (BG, Z,
+each (early stop on for both; batches of 16,384 codewords, the batch of the
+learned-vs-plain configuration).  ``mixed_batch`` times the uneven (BG, Z,
 rate-matched) 8192-codeword workload in one launch; ``training`` the learned
 decoder's training step (BG2 Z=128, 8 iterations, 16384 codewords);
 ``c1_fer_curve`` the FER curve of the bench code over Eb/N0 0.5-2.5 dB;
@@ -171,11 +172,12 @@ def run_e2e(dec, llr, packed, steps, stream, world, mode="auto"):
     return e2e_ms
 
 
-def learned_vs_plain(dec, stream, batch: int, ebn0: float = 1.8, frames: int = 65536,
-                     timed_steps: int = 10):
+def learned_vs_plain(stream, batch: int = 16384, ebn0: float = 1.8, frames: int = 65536,
+                     timed_steps: int = 10, device: int = 0):
     """The learned decoder against plain min-sum at one stated Eb/N0 (1.8 dB,
     where plain flooding min-sum at 10 iterations has FER <= 1e-2), early stop
-    on for both, `frames` fresh codewords per configuration:
+    on for both, `frames` fresh codewords per configuration, decoded and
+    timed in batches of 16384 (the learned-vs-plain configuration's batch):
       plain   - the reference's decoder: flooding, alpha 0.75, 10 iterations;
       learned - layered weighted min-sum with the GPU-trained weights
                 weights/bg1_L6, at the smallest cap in 4..6 iterations whose
@@ -185,9 +187,10 @@ def learned_vs_plain(dec, stream, batch: int, ebn0: float = 1.8, frames: int = 6
     weights (alpha 0.75) at the learned cap, and the flooding decoder with
     its own trained weights (weights/bg1_T10) at 10 iterations."""
     import torch
-    from nr_gpu_ldpc_gb300 import codes
+    from nr_gpu_ldpc_gb300 import Decoder, codes
     from nr_gpu_ldpc_gb300.evaluate import clopper_pearson
     from nr_gpu_ldpc_gb300.learned import load_weights
+    dec = Decoder(bg=BG, z=Z, max_batch=batch, device=device)
     sigma = codes.noise_sigma(ebn0, K_INFO / (N_BP - 2 * Z))
     sig = torch.full((batch,), sigma, dtype=torch.float32, device="cuda")
     out = torch.empty((batch, dec.packed_bytes), dtype=torch.uint8, device="cuda")
@@ -238,7 +241,8 @@ def learned_vs_plain(dec, stream, batch: int, ebn0: float = 1.8, frames: int = 6
            "speedup": learned["info_gbps"] / plain["info_gbps"],
            "layered_without_weights": run("layered", None, learned["iters_max"]),
            "flooding_learned_T10": run("flooding", "bg1_T10", ITERS)}
-    dec.set_schedule("flooding")
+    res["batch"] = batch
+    dec.close()
     return res, launches
 
 
@@ -516,7 +520,7 @@ def main():
             except Exception as exc:  # noqa: BLE001
                 e2e_modes[mode] = f"{type(exc).__name__}: {exc}"
 
-    lvp, lvp_launches = (None, 0) if args.no_learned else learned_vs_plain(dec, stream, min(B, 4096))
+    lvp, lvp_launches = (None, 0) if args.no_learned else learned_vs_plain(stream, device=local)
     extra = {}
     if not args.no_extra and rank == 0:
         for name, leg in (("mixed_batch", lambda: mixed_batch(stream)), ("training", training_step),
