@@ -51,6 +51,12 @@ __device__ __forceinline__ float wsel(const float4* w, int i) {
     return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w;
 }
 constexpr long kWaitLimit = 1L << 20;
+// Early stop: per-slot row of the last failed syndrome check, kFarOffset ints
+// after the per-slot fail flags in the header (both kernels: flags at byte
+// 16, up to kMaxCpb of each, header 1024 bytes); from row kFarRow on, the next
+// check is bit-sliced.
+constexpr int kFarOffset = 60;
+constexpr int kFarRow = 12;
 
 __device__ __forceinline__ float max_nan(float a, float b) {
     float r;
@@ -374,9 +380,9 @@ __device__ __forceinline__ void iterate_rows(const CodeTable& tab, uint32_t s, u
 // just written (s4a: its shared address plus 4*s), suffix columns from bit 1
 // of their hard-decision bytes.  Threads stop at the first failure seen by
 // any thread of the slot, so an iteration far from convergence costs a few
-// rows.
+// rows; *far gets the row of the failure.
 __device__ __forceinline__ void check_rows(const CodeTable& tab, uint32_t s, uint32_t s4a, uint32_t hd_base,
-                                           volatile int* fail) {
+                                           volatile int* fail, int* far) {
     const int z = tab.z;
     const uint32_t z4 = 4u * static_cast<uint32_t>(z);
     for (int r = 0; r < tab.rows; r++) {
@@ -390,8 +396,103 @@ __device__ __forceinline__ void check_rows(const CodeTable& tab, uint32_t s, uin
         }
         if (par) {
             *fail = 1;
+            *far = r;
             return;
         }
+    }
+}
+
+// Four suffix hard decisions (bit 1 of four consecutive bytes, little-endian)
+// moved into the top nibble of acc, which shifts down by four: after eight
+// words the nibble of the first word sits at bits 0..3.
+__device__ __forceinline__ uint32_t sfx_nibble(uint32_t w, uint32_t acc) {
+    // the multiply moves bits 1, 9, 17, 25 to 28, 29, 30, 31 (no carries)
+    return (acc >> 4) | (((w & 0x02020202u) * 0x08102040u) & 0xf0000000u);
+}
+
+// Syndrome of every slot after an iteration, 32 sub-rows at a time (Z a
+// multiple of 32; same hard-decision rule as check_rows).  The core hard
+// decisions of the posterior just written (lnew0: slot 0, slots cf floats
+// apart) are packed into words, each column block stored twice in a row so
+// that a 32-bit window never wraps: word x of block c of slot j
+// (bits + (j*n_core + c)*2*nw + x, nw = Z/32) holds the decisions of
+// positions c*Z + 32*(x mod nw) + 0..31.  Then, for (slot j, row r, word k),
+// the XOR over the row's core edges (column c, shift V) of the window of
+// block c that starts at bit (32k + V) mod Z -- the decisions the sub-rows
+// 32k..32k+31 see -- and of the suffix decisions of those sub-rows (bit 1 of
+// their bytes in hd0, slots rows*Z bytes apart) is nonzero exactly when one
+// of these lifted checks fails (a failing slot's s_far is set to rows).  The table entries these tasks need are
+// copied next to the packed words first (edge: window word offset
+// c*2*nw + V/32 and bit offset V mod 32 in 16 bits; row: first and end core
+// edge, suffix flag), so every lane can take a task of its own.  Every
+// thread of the CTA calls it (one barrier inside); the scratch is
+// cpb*n_core*2*nw words + rows words + n_edges halfwords.
+__device__ __forceinline__ void check_bits(const CodeTable& tab, int cpb, const float* lnew0, const uint8_t* hd0,
+                                           uint32_t* bits, int* s_fail, int* s_far) {
+    const int z = tab.z, nw = z >> 5, rows = tab.rows, nc = tab.n_core;
+    const int tid = static_cast<int>(threadIdx.x), nt = static_cast<int>(blockDim.x);
+    uint32_t* rinfo = bits + cpb * nc * 2 * nw;               // [rows]
+    uint16_t* einfo = reinterpret_cast<uint16_t*>(rinfo + rows);  // [n_edges]
+    for (int e = tid; e < tab.n_edges; e += nt) {
+        const uint32_t v = tab.edge_shift[e];
+        einfo[e] = static_cast<uint16_t>(((tab.edge_col[e] * 2u * nw + (v >> 5)) << 5) | (v & 31u));
+    }
+    for (int r = tid; r < rows; r += nt) {
+        const uint32_t sfx = tab.row_sfx[r] ? 1u : 0u;
+        rinfo[r] = tab.row_ptr[r] | ((tab.row_ptr[r + 1] - sfx) << 16) | (sfx << 31);
+    }
+    {   // pack: thread = word x of blocks bc0, bc0 + step, ... (bc = j*nc + c).
+        // The words of a warp's lanes start 128 bytes apart (one bank), so
+        // lane t reads its 32 posteriors starting at the t-th (all 32 banks
+        // per load) and rotates the collected word back by t.
+        const int x = tid % nw, step = nt / nw, rot = tid & 31;
+        for (int bc = tid / nw; bc < cpb * nc && tid < step * nw; bc += step) {
+            const float* src = lnew0 + static_cast<size_t>(bc) * z + 32 * x;
+            uint32_t w = 0;  // bit i: decision of position (i + rot) mod 32
+#pragma unroll
+            for (int i = 0; i < 32; i++) w |= (src[(i + rot) & 31] > 0.0f ? 0u : 1u) << i;
+            w = __funnelshift_l(w, w, static_cast<uint32_t>(rot));
+            uint32_t* dst = bits + bc * 2 * nw + x;
+            dst[0] = w;
+            dst[nw] = w;
+        }
+    }
+    __syncthreads();
+    // tasks: thread = (slot, word) pair jk of rows r0, r0 + step, ...
+    const int pairs = cpb * nw, step = nt / pairs, jk = tid % pairs;
+    if (tid >= step * pairs) return;
+    const int j = jk / nw, k = jk - j * nw;
+    const uint32_t* wb = bits + j * nc * 2 * nw + k;
+    const uint8_t* hj = hd0 + static_cast<size_t>(j) * rows * z + 32 * k;
+    uint32_t fail = 0;
+    for (int r = tid / pairs; r < rows; r += step) {
+        const uint32_t ri = rinfo[r];
+        uint32_t acc = 0;
+#pragma unroll 4
+        for (int e = static_cast<int>(ri & 0xffffu); e < static_cast<int>((ri >> 16) & 0x7fffu); e++) {
+            const uint32_t ei = einfo[e];
+            const uint32_t* w = wb + (ei >> 5);
+            acc ^= __funnelshift_r(w[0], w[1], ei & 31u);
+        }
+        if (ri >> 31) {
+            const uint4* h = reinterpret_cast<const uint4*>(hj + r * z);
+            const uint4 h0 = h[0], h1 = h[1];
+            uint32_t sb = 0;
+            sb = sfx_nibble(h0.x, sb);
+            sb = sfx_nibble(h0.y, sb);
+            sb = sfx_nibble(h0.z, sb);
+            sb = sfx_nibble(h0.w, sb);
+            sb = sfx_nibble(h1.x, sb);
+            sb = sfx_nibble(h1.y, sb);
+            sb = sfx_nibble(h1.z, sb);
+            sb = sfx_nibble(h1.w, sb);
+            acc ^= sb;
+        }
+        fail |= acc;
+    }
+    if (fail) {
+        s_fail[j] = 1;
+        s_far[j] = rows;  // a failing slot keeps the bit-sliced check
     }
 }
 
@@ -416,6 +517,7 @@ __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slo
                                           int n_iter, int early_stop, float alpha, const float* wtab, float4* wpad,
                                           int n_w_iters) {
     const int z = tab.z, cf = tab.core_floats, tid = threadIdx.x;
+    int* s_far = s_fail + kFarOffset;  // per slot: row of the last failed check
     float* lold = buf0 + static_cast<size_t>(slot) * cf;  // read by the check-node pass
     float* lnew = LAYERED ? lold : lold + static_cast<size_t>(cpb) * cf;  // the posterior written
     const uint8_t* hd = hd0 + static_cast<size_t>(slot) * tab.rows * z;
@@ -443,13 +545,27 @@ __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slo
             }
         }
         if (tid < cpb) s_fail[tid] = 0;
-        __syncthreads();
+        // the syndrome pass of this iteration: bit-sliced when a codeword of
+        // the CTA failed its previous check at row kFarRow or later (near
+        // convergence: a row-by-row scan would run through most rows), else
+        // row by row with an early exit (s_far was written before the
+        // previous iteration's closing barriers)
+        const bool far_check = __syncthreads_or(!slot_done && s_far[slot] >= kFarRow);
         const bool act = !slot_done;
         const bool store = !last || out.app != nullptr;
         iterate_rows<WEIGHTED, LAYERED>(tab, s, s4old, dnew, wpad, st_base, gllr, hd_base, act, first, store,
                                         early_stop || last, alpha);
         if (early_stop && !last) {  // the rows ended with a barrier
-            if (act) check_rows(tab, s, s4old + dnew, hd_base, &s_fail[slot]);
+            // bit-sliced scratch: flooding in Lold (read again only after the
+            // copy-back below), layered in the weight rows (restaged at the
+            // next iteration's start)
+            const int scratch = cpb * tab.n_core * (z >> 4) + tab.rows + (tab.n_edges + 1) / 2;
+            if (far_check && (z & 31) == 0 && scratch <= (LAYERED ? kWeightBytes / 4 : cpb * cf))
+                check_bits(tab, cpb, lnew - static_cast<size_t>(slot) * cf, hd0,
+                           LAYERED ? reinterpret_cast<uint32_t*>(wpad) : reinterpret_cast<uint32_t*>(buf0), s_fail,
+                           s_far);
+            else if (act)
+                check_rows(tab, s, s4old + dnew, hd_base, &s_fail[slot], &s_far[slot]);
             __syncthreads();
             const bool conv = act && s_fail[slot] == 0;
             if (conv)  // HD of this iteration is a codeword
@@ -466,6 +582,7 @@ __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slo
                 reinterpret_cast<float4*>(lold)[k] = reinterpret_cast<const float4*>(lnew)[k];
     }
     __syncthreads();  // buffers are rewritten by the next group's copy
+    if (tid < cpb) s_far[tid] = 0;  // read again only after the next group's barriers
 }
 
 // MINB = CTAs per SM the register budget is sized for: 1 when shared memory
@@ -507,6 +624,7 @@ __global__ void __launch_bounds__(kMaxThreads, MINB)
         mbar_init(bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    if (threadIdx.x < kMaxCpb) s_fail[kFarOffset + threadIdx.x] = 0;
     __syncthreads();
     uint32_t phase = 0;
 
@@ -573,6 +691,7 @@ __global__ void __launch_bounds__(kMaxThreads, 2)
         mbar_init(bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    if (threadIdx.x < kMaxCpb) s_fail[kFarOffset + threadIdx.x] = 0;
     __syncthreads();
     uint32_t phase = 0;
     for (;;) {
