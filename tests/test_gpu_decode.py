@@ -351,3 +351,37 @@ def test_bounded_wait_reports_timeout(gpu):
     assert np.array_equal(packed.cpu().numpy(), want)
     assert dec.device_error() == 0
     dec.close()
+
+
+@pytest.mark.parametrize("schedule", ["flooding", "layered-learned"])
+def test_early_stop_parity_across_the_waterfall(gpu, schedule):
+    """Early stop where it matters most: 96 BG1 Z=384 codewords spread over
+    the waterfall (1.7-1.9 dB), many of which converge after a few to many
+    iterations and fail their syndrome checks at late rows first -- the
+    state in which the decoder switches from the row-by-row syndrome pass to
+    the bit-sliced one.  Iteration counts, hard decisions and posteriors
+    equal the oracle's (plain flooding min-sum, or the layered decoder with
+    the trained weights bg1_L6)."""
+    from nr_gpu_ldpc_gb300.learned import load_weights
+    z, n = 384, 96
+    dec = make_decoder(1, z, max_batch=n)
+    oc = oracle_for(dec)
+    sig = np.array([codes.noise_sigma(eb, 1 / 3) for eb in np.linspace(1.7, 1.9, n)], np.float32)
+    llr, _ = oc.gen_llr(dec.kb, 4242, 0, sig, 2)
+    d = torch.from_numpy(llr).to(gpu)
+    if schedule == "flooding":
+        pk, app, its = dec.decode(d, 15, early_stop=True, want_app=True, want_iters=True)
+        torch.cuda.synchronize()
+        opk, oapp, oits = oc.minsum_f32(llr, 15, early_stop=True, want_app=True, threads=4)
+    else:
+        w = load_weights("bg1_L6")
+        dec.set_schedule("layered")
+        dec.set_weights(w)
+        pk, app, its = dec.decode(d, 6, early_stop=True, weighted=True, want_app=True, want_iters=True)
+        torch.cuda.synchronize()
+        opk, oapp, oits = oc.layered_f32(llr, 6, w=w, early_stop=True, want_app=True, threads=4)
+    np.testing.assert_array_equal(its.cpu().numpy(), oits)
+    np.testing.assert_array_equal(pk.cpu().numpy(), opk)
+    np.testing.assert_array_equal(app.cpu().numpy().view(np.uint32), oapp.view(np.uint32))
+    assert len(np.unique(oits)) >= 2  # codewords stop at different iterations
+    dec.close()
