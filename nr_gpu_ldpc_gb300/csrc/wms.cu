@@ -40,12 +40,16 @@ __device__ __forceinline__ float max_nan(float a, float b) {
     return r;
 }
 
-__device__ __forceinline__ float softplus_f(float z) {
-    return z > 0.0f ? z + log1pf(expf(-z)) : log1pf(expf(z));
-}
-__device__ __forceinline__ float sigmoid_f(float z) { return 1.0f / (1.0f + expf(-z)); }
 
 __device__ __forceinline__ int cw_bit(const uint8_t* cw, int c) { return (cw[c >> 3] >> (c & 7)) & 1; }
+
+// The stored states of a chunk (hundreds of MB per iteration) do not stay in
+// L2: a row's state is pulled into L2 kPrefetchRows rows before its
+// register load, which runs two rows ahead.
+constexpr int kPrefetchRows = 6;
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
 
 // ---- forward ------------------------------------------------------------------------
 template <int D, bool LAYERED>
@@ -159,9 +163,22 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
         const bool act = valid && cw < a.n_cw;
         float* lold = bufs + static_cast<size_t>(slot) * n;
         float* lnew = LAYERED ? lold : bufs + static_cast<size_t>(cpb + slot) * n;
+        // this thread's codeword bits at positions s, s + Z, s + 2Z, ... (at
+        // most kMaxCols of them) as a 128-bit mask, read once per group
+        uint64_t ybits0 = 0, ybits1 = 0;
         if (act) {
             const float4* src = reinterpret_cast<const float4*>(a.llr + static_cast<size_t>(cw) * n);
+#pragma unroll 4
             for (int k = static_cast<int>(s); k < n / 4; k += z) reinterpret_cast<float4*>(lold)[k] = src[k];
+            const uint8_t* bits = a.cw + static_cast<size_t>(cw) * tab.packed_bytes;
+#pragma unroll 4
+            for (int k = 0; k < tab.cols; k++) {
+                const uint64_t b = static_cast<uint64_t>(cw_bit(bits, static_cast<int>(s) + k * z));
+                if (k < 64)
+                    ybits0 |= b << k;
+                else
+                    ybits1 |= b << (k - 64);
+            }
         }
         float loss_part = 0.0f;
         for (int t = 0; t < a.T; t++) {
@@ -183,7 +200,10 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
                 return (act && t > 0 && r < rows) ? __ldcg(st_prev + r * z + s) : make_uint4(0u, 0u, 0u, 0u);
             };
             uint4 p0 = fetch(0), p1 = fetch(1);
+            if (act && t > 0)
+                for (int r = 2; r < kPrefetchRows && r < rows; r++) prefetch_l2(st_prev + r * z + s);
             for (int r = 0; r < rows; r++) {
+                if (act && t > 0 && r + kPrefetchRows < rows) prefetch_l2(st_prev + (r + kPrefetchRows) * z + s);
                 const uint4 p2 = fetch(r + 2);
                 if (act)
                     fwd_dispatch<LAYERED>(tab.row_deg[r], tab, tab.row_ptr[r], s, lold, lnew, wbuf,
@@ -194,13 +214,21 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
             }
             // loss term and its gradient seed at L^{t+1}
             if (act) {
-                const uint8_t* bits = a.cw + static_cast<size_t>(cw) * tab.packed_bytes;
                 float* seed = a.gseed + (static_cast<size_t>(t) * a.n_cw + cw) * n;
+                uint64_t y0 = ybits0, y1 = ybits1;
+                // softplus(zz) = max(zz, 0) + log1p(e) and sigmoid(zz) =
+                // 1/(1 + e) (zz >= 0) or e/(1 + e) (zz < 0), e = exp(-|zz|):
+                // one exponential per position
+#pragma unroll 4
                 for (int c = static_cast<int>(s); c < n; c += z) {
-                    const float y = cw_bit(bits, c) ? -1.0f : 1.0f;
+                    const float y = (y0 & 1u) ? -1.0f : 1.0f;
+                    y0 = (y0 >> 1) | (y1 << 63);
+                    y1 >>= 1;
                     const float zz = -y * lnew[c];
-                    loss_part += softplus_f(zz);
-                    seed[c] = a.scale * (-y) * sigmoid_f(zz);
+                    const float e = expf(-fabsf(zz));
+                    loss_part += fmaxf(zz, 0.0f) + log1pf(e);
+                    const float r = __frcp_rn(1.0f + e);
+                    seed[c] = a.scale * (-y) * (zz >= 0.0f ? r : e * r);
                 }
             }
             float* tmp = lold;
@@ -341,6 +369,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
         float* gln = bufs + static_cast<size_t>(cpb + slot) * n;    // dloss/dL^t
         if (act) {
             const float* seed = a.gseed + (static_cast<size_t>(a.T - 1) * a.n_cw + cw) * n;
+#pragma unroll 4
             for (int c = static_cast<int>(s); c < n; c += z) gl[c] = seed[c];
             for (int k = 0; k < rows; k++) gq[k * z + s] = make_uint4(0u, 0u, 31u, 31u);
         }
@@ -352,6 +381,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
             if (act) {
                 if (t > 0) {
                     const float* seed = a.gseed + (static_cast<size_t>(t - 1) * a.n_cw + cw) * n;
+#pragma unroll 4
                     for (int c = static_cast<int>(s); c < n; c += z) gln[c] = seed[c];
                 }
             }
@@ -369,7 +399,16 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
             uint4 s0, g0, s1, g1;
             fetch(0, s0, g0);
             fetch(1, s1, g1);
+            if (act)
+                for (int r = 2; r < kPrefetchRows && r < rows; r++) {
+                    prefetch_l2(st + r * z + s);
+                    prefetch_l2(gq + r * z + s);
+                }
             for (int r = 0; r < rows; r++) {
+                if (act && r + kPrefetchRows < rows) {
+                    prefetch_l2(st + (r + kPrefetchRows) * z + s);
+                    prefetch_l2(gq + (r + kPrefetchRows) * z + s);
+                }
                 uint4 s2, g2;
                 fetch(r + 2, s2, g2);
                 bwd_dispatch(tab.row_deg[r], tab, tab.row_ptr[r], s, act, gl, gln, wcur, gw_acc, s0, g0,
@@ -481,6 +520,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
             }
             if (act) {
                 const float* seed = a.gseed + (static_cast<size_t>(t) * a.n_cw + cw) * n;
+#pragma unroll 4
                 for (int c = static_cast<int>(s); c < n; c += z) g[c] += seed[c];
             }
             __syncthreads();
@@ -489,7 +529,10 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
                 return (act && r >= 0) ? __ldcg(st + r * z + s) : make_uint4(0u, 0u, 0u, 31u);
             };
             uint4 s0 = fetch(rows - 1), s1 = fetch(rows - 2);
+            if (act)
+                for (int r = rows - 3; r > rows - 1 - kPrefetchRows && r >= 0; r--) prefetch_l2(st + r * z + s);
             for (int r = rows - 1; r >= 0; r--) {
+                if (act && r - kPrefetchRows >= 0) prefetch_l2(st + (r - kPrefetchRows) * z + s);
                 const uint4 s2 = fetch(r - 2);
                 bwd_layered_dispatch(tab.row_deg[r], tab, tab.row_ptr[r], s, act, g, wcur, gw_acc, s0,
                                      gh + static_cast<size_t>(tab.row_ptr[r]) * z + s, t < a.T - 1, t > 0);
