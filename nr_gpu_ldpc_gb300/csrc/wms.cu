@@ -43,14 +43,6 @@ __device__ __forceinline__ float max_nan(float a, float b) {
 
 __device__ __forceinline__ int cw_bit(const uint8_t* cw, int c) { return (cw[c >> 3] >> (c & 7)) & 1; }
 
-// The stored states of a chunk (hundreds of MB per iteration) do not stay in
-// L2: a row's state is pulled into L2 kPrefetchRows rows before its
-// register load, which runs two rows ahead.
-constexpr int kPrefetchRows = 6;
-__device__ __forceinline__ void prefetch_l2(const void* p) {
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-}
-
 // ---- forward ------------------------------------------------------------------------
 template <int D, bool LAYERED>
 __device__ __forceinline__ void fwd_row(const CodeTable& tab, int e0, uint32_t s, const float* lold,
@@ -200,10 +192,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
                 return (act && t > 0 && r < rows) ? __ldcg(st_prev + r * z + s) : make_uint4(0u, 0u, 0u, 0u);
             };
             uint4 p0 = fetch(0), p1 = fetch(1);
-            if (act && t > 0)
-                for (int r = 2; r < kPrefetchRows && r < rows; r++) prefetch_l2(st_prev + r * z + s);
             for (int r = 0; r < rows; r++) {
-                if (act && t > 0 && r + kPrefetchRows < rows) prefetch_l2(st_prev + (r + kPrefetchRows) * z + s);
                 const uint4 p2 = fetch(r + 2);
                 if (act)
                     fwd_dispatch<LAYERED>(tab.row_deg[r], tab, tab.row_ptr[r], s, lold, lnew, wbuf,
@@ -399,16 +388,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
             uint4 s0, g0, s1, g1;
             fetch(0, s0, g0);
             fetch(1, s1, g1);
-            if (act)
-                for (int r = 2; r < kPrefetchRows && r < rows; r++) {
-                    prefetch_l2(st + r * z + s);
-                    prefetch_l2(gq + r * z + s);
-                }
             for (int r = 0; r < rows; r++) {
-                if (act && r + kPrefetchRows < rows) {
-                    prefetch_l2(st + (r + kPrefetchRows) * z + s);
-                    prefetch_l2(gq + (r + kPrefetchRows) * z + s);
-                }
                 uint4 s2, g2;
                 fetch(r + 2, s2, g2);
                 bwd_dispatch(tab.row_deg[r], tab, tab.row_ptr[r], s, act, gl, gln, wcur, gw_acc, s0, g0,
@@ -529,10 +509,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
                 return (act && r >= 0) ? __ldcg(st + r * z + s) : make_uint4(0u, 0u, 0u, 31u);
             };
             uint4 s0 = fetch(rows - 1), s1 = fetch(rows - 2);
-            if (act)
-                for (int r = rows - 3; r > rows - 1 - kPrefetchRows && r >= 0; r--) prefetch_l2(st + r * z + s);
             for (int r = rows - 1; r >= 0; r--) {
-                if (act && r - kPrefetchRows >= 0) prefetch_l2(st + (r - kPrefetchRows) * z + s);
                 const uint4 s2 = fetch(r - 2);
                 bwd_layered_dispatch(tab.row_deg[r], tab, tab.row_ptr[r], s, act, g, wcur, gw_acc, s0,
                                      gh + static_cast<size_t>(tab.row_ptr[r]) * z + s, t < a.T - 1, t > 0);
