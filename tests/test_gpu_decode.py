@@ -249,6 +249,13 @@ def test_host_call_in_chunks_back_to_back(gpu):
     dec.decode_host_q(q.pin_memory(), out_q, 7, stream=s)
     s.synchronize()
     assert torch.equal(out_q, dec.decode(q.to(gpu).float(), 7).cpu())
+    # int8 with a scale: widened on the GPU on whichever lane decodes the chunk
+    scale = 0.125
+    q8 = torch.clamp(torch.round(llr_b.cpu() / scale), -128, 127).to(torch.int8)
+    out_8 = torch.empty_like(out_a).pin_memory()
+    dec.decode_host_q(q8.pin_memory(), out_8, 7, scale=scale, stream=s)
+    s.synchronize()
+    assert torch.equal(out_8, dec.decode((q8.to(gpu).float() * scale).contiguous(), 7).cpu())
 
 
 @pytest.mark.parametrize("bg,z,n,early", [(1, 384, 700, False), (2, 52, 333, True)])
