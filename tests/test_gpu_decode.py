@@ -258,7 +258,7 @@ def test_host_call_in_chunks_back_to_back(gpu):
     assert torch.equal(out_8, dec.decode((q8.to(gpu).float() * scale).contiguous(), 7).cpu())
 
 
-@pytest.mark.parametrize("bg,z,n,early", [(1, 384, 700, False), (2, 52, 333, True)])
+@pytest.mark.parametrize("bg,z,n,early", [(1, 384, 700, False), (1, 384, 700, True), (2, 52, 333, True)])
 def test_host_transfer_modes_agree(gpu, bg, z, n, early):
     """'direct' (the decoder reads pinned host LLRs and writes the packed bits
     back itself), 'copy' (staged chunks) and 'auto' all give the device
