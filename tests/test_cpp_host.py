@@ -65,3 +65,25 @@ def test_reference_call_shape_decodes_like_the_oracle(tmp_path, cuda_lib):
     assert r.returncode == 0, r.stderr
     want, _, _ = oc.minsum_f32(llr, 10)
     np.testing.assert_array_equal(np.fromfile(dst, np.uint8).reshape(want.shape), want)
+
+
+@pytest.mark.gpu
+def test_cpp_caller_two_lane_pipeline(tmp_path, cuda_lib):
+    """The C++ caller on a batch of more than one CTA round with staged copies:
+    the chunks decode on both of the handle's lanes (the caller's stream and
+    the handle's own), and the packed bits equal the device-resident decode
+    of the same LLRs."""
+    import torch
+    from nr_gpu_ldpc_gb300 import Decoder
+    exe = _build(tmp_path, cuda_lib)
+    n = 330  # BG1 Z=384 on a GB300: a 304-codeword round, then 26 more
+    dec = Decoder(bg=1, z=384, max_batch=n)
+    sig = torch.full((n,), codes.noise_sigma(1.7, 1 / 3), device="cuda")
+    llr, _ = dec.gen_llr(71, 0, sig)
+    want = dec.decode(llr, 10).cpu().numpy()
+    dec.close()
+    src, dst = tmp_path / "llr.f32", tmp_path / "out.u8"
+    llr.cpu().numpy().tofile(src)
+    r = subprocess.run([exe, "8424", "10", str(src), str(dst), "1"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    np.testing.assert_array_equal(np.fromfile(dst, np.uint8).reshape(want.shape), want)
