@@ -378,26 +378,48 @@ def c0_default_code(n: int = 640, n_iter: int = 5, reps: int = 20):
                                 "(GeForce GTX 950M, its original 12x24 code)"}
 
 
-def cpu_baseline(llr_host: np.ndarray, n_sample: int):
+def cpu_model() -> str:
+    """Host CPU model as lscpu names it (e.g. Neoverse-V2 on Grace)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def cpu_baseline(llr_host: np.ndarray, n_sample: int, runs: int = 5):
     """Reference algorithm on the host cores: the oracle's C restatement of
-    the reference min-sum (kind 'port'), all cores, one codeword per thread."""
+    the reference min-sum (kind 'port'), all cores with one codeword per
+    thread, and one thread; median of `runs` timed runs each (steady clock)."""
     from nr_gpu_ldpc_gb300 import codes
     from oracle.oracle import OracleCode
     oc = OracleCode(codes.base_matrix(BG, codes.set_index(Z)), Z)
     cores = os.cpu_count() or 1
     sample = np.ascontiguousarray(llr_host[:n_sample])
     oc.minsum_f32(sample[:cores], 1, threads=cores)  # warm
-    t0 = time.perf_counter()
-    oc.minsum_f32(sample, ITERS, threads=cores)
-    dt = time.perf_counter() - t0
-    n1 = min(8, n_sample)
-    t0 = time.perf_counter()
-    oc.minsum_f32(sample[:n1], ITERS, threads=1)
-    dt1 = time.perf_counter() - t0
+
+    def median_s(x, threads):
+        ts = []
+        for _ in range(runs):
+            t0 = time.perf_counter()
+            oc.minsum_f32(x, ITERS, threads=threads)
+            ts.append(time.perf_counter() - t0)
+        return statistics.median(ts), ts
+
+    dt, ts = median_s(sample, cores)
+    n1 = min(16, n_sample)
+    dt1, _ = median_s(sample[:n1], 1)
     return {"value": n_sample * K_INFO / dt / 1e9, "unit": "Gbit/s", "cores": cores, "kind": "port",
+            "cpu_model": cpu_model(), "runs": runs, "statistic": "median",
             "sample": f"{n_sample} BG1 Z=384 codewords of the bench batch, {ITERS} iterations, "
-                      f"{cores} threads ({dt:.2f} s)",
-            "value_1thread": n1 * K_INFO / dt1 / 1e9}
+                      f"{cores} threads, median of {runs} runs ({dt:.2f} s each; "
+                      f"range {min(ts):.2f}-{max(ts):.2f} s)",
+            "value_1thread": n1 * K_INFO / dt1 / 1e9,
+            "sample_1thread": f"{n1} codewords on 1 thread, median of {runs} runs ({dt1:.3f} s)"}
 
 
 def workload_config(batch: int) -> dict:
@@ -429,7 +451,7 @@ def run_reference(args, world, rank):
         t0 = time.perf_counter()
         oc.minsum_f32(llr, ITERS, threads=cores)
         times.append(time.perf_counter() - t0)
-    ms = 1e3 * sum(times) / len(times)
+    ms = 1e3 * statistics.median(times)
     value = n_step * K_INFO / (ms * 1e-3) / 1e9
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Gbit/s",
@@ -438,6 +460,7 @@ def run_reference(args, world, rank):
         "data": "synthetic (seeded Philox info bits, BPSK/AWGN LLRs)",
         "config": dict(workload_config(BATCH), reference_sample_codewords_per_step=n_step, threads=cores),
         "cpu_baseline": {"value": value, "unit": "Gbit/s", "cores": cores, "kind": "port",
+                         "cpu_model": cpu_model(), "statistic": f"median of {args.steps} steps",
                          "sample": f"{n_step} codewords per step on {cores} threads"},
         "e2e": {"value": value, "unit": "Gbit/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }

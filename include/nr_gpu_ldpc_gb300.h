@@ -254,13 +254,36 @@ int nrldpc_rm_k0(int bg, int z, int rv);
  * another runtime's memory manager -- and so cannot hold an nrldpc_handle.
  * Same results as nrldpc_decode for 5G NR (bg, z) with alpha (device
  * pointers, 16-byte aligned d_llr; packed output as nrldpc_decode).  Scratch
- * is one static 96 MiB device array in the library, held by a GPU from the
- * first call on it until the process exits; a code whose per-CTA check-node
- * state does not fit returns NRLDPC_ERR_SCRATCH_TOO_SMALL.  The first call on
- * a device (the current one) sets it up: make it before any stream capture.
- * Calls share the array: calls that overlap on the GPU race; serialise them. */
+ * is one static 96 MiB device array in the library; a code whose per-CTA
+ * check-node state does not fit returns NRLDPC_ERR_SCRATCH_TOO_SMALL.  A GPU
+ * reserves the array when the runtime loads the library module that holds
+ * it, and keeps it until the process exits: under lazy module loading (the
+ * default) at the first call on that GPU that touches it (this entry point
+ * or nrldpc_noalloc_device_error), under CUDA_MODULE_LOADING=EAGER at
+ * context creation on every GPU the process uses -- whether or not this
+ * entry point is ever called.  The first
+ * successful call on a device (the current one) sets it up: make it before
+ * any stream capture; a failed set-up is retried by the next call.  Calls
+ * share the array: calls that overlap on the GPU race; serialise them.
+ * A bounded device-side wait that ran out is reported by
+ * nrldpc_noalloc_device_error, not by this call's return value. */
 int nrldpc_decode_noalloc(int bg, int z, float alpha, const float* d_llr, uint8_t* d_packed,
                           int n_cw, int n_iter, int early_stop, nrldpc_stream_t stream);
+
+/* Device-side error of nrldpc_decode_noalloc calls on the current device
+ * since the last query (NRLDPC_ERR_TIMEOUT when a bounded wait ran out, the
+ * call's output then unwritten; NRLDPC_OK otherwise), and clears it.  A
+ * synchronous symbol copy, no allocation: synchronise the decode's stream
+ * first.  No reference counterpart (the reference checks no kernel error). */
+int nrldpc_noalloc_device_error(void);
+
+/* Self-test of nrldpc_decode_noalloc's bounded wait (no reference
+ * counterpart), as nrldpc_selftest_wait_timeout for a handle: one iteration
+ * whose copy barrier expects 16 bytes that no copy delivers (no copy is
+ * issued), with a short wait limit; nrldpc_noalloc_device_error then returns
+ * NRLDPC_ERR_TIMEOUT.  Nothing faults or spins without end. */
+int nrldpc_selftest_noalloc_wait_timeout(int bg, int z, const float* d_llr, uint8_t* d_packed, int n_cw,
+                                         nrldpc_stream_t stream);
 
 /* CRC (3GPP TS 38.212 5.1) of the first n_bits of each of n_cw packed
  * words (stride_bytes apart); bit i of the packed bytes is the i-th bit of
@@ -297,12 +320,12 @@ int nrldpc_device_error(nrldpc_handle* h);
 
 /* Self-test of the bounded device-side wait (no reference counterpart): one
  * device-resident decode of n_cw codewords whose copy barrier is told to
- * expect 16 bytes more than the LLR copies deliver, with a short wait limit.
- * Every CTA's wait for its first codeword runs out, the kernel records the
- * timeout (nrldpc_device_error then returns NRLDPC_ERR_TIMEOUT) and its CTAs
- * return without writing d_packed.  Nothing faults or spins without end: the
- * copies land, only the barrier's phase never completes.  The handle stays
- * usable. */
+ * expect 16 bytes more than the LLR copies deliver, with a short wait limit;
+ * no copy is issued, so nothing is in flight when the wait runs out.  Every
+ * CTA's wait for its first codeword runs out, the kernel records the timeout
+ * (nrldpc_device_error then returns NRLDPC_ERR_TIMEOUT) and its CTAs return
+ * without writing d_packed.  Nothing faults or spins without end.  The
+ * handle stays usable. */
 int nrldpc_selftest_wait_timeout(nrldpc_handle* h, const float* d_llr, uint8_t* d_packed, int n_cw,
                                  nrldpc_stream_t stream);
 

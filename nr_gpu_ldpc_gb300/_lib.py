@@ -80,6 +80,8 @@ SIGNATURES = {
     "nrldpc_decode_noalloc": (_i, [_i, _i, _f, _vp, _vp, _i, _i, _i, _vp]),
     "nrldpc_device_error": (_i, [_vp]),
     "nrldpc_selftest_wait_timeout": (_i, [_vp, _vp, _vp, _i, _vp]),
+    "nrldpc_noalloc_device_error": (_i, []),
+    "nrldpc_selftest_noalloc_wait_timeout": (_i, [_i, _i, _vp, _vp, _i, _vp]),
     "nrldpc_status_string": (C.c_char_p, [_i]),
 }
 

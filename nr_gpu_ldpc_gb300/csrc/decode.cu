@@ -652,15 +652,23 @@ __global__ void __launch_bounds__(kMaxThreads, MINB)
             if (tid == 0) {  // core-column LLRs of each codeword into its Lold
                 fence_proxy_async();
                 mbar_arrive_expect_tx(bar, static_cast<uint32_t>(n_valid) * cf * 4u + a.extra_tx);
-                for (int k = 0; k < n_valid; k++)
-                    bulk_g2s(smem_addr(buf0 + static_cast<size_t>(k) * cf),
-                             a.llr + static_cast<size_t>(cw0 + k) * n, cf * 4u, bar);
+                // the timeout self-test (extra_tx != 0) expects bytes but
+                // issues no copy, so nothing is in flight when its wait runs out
+                if (a.extra_tx == 0)
+                    for (int k = 0; k < n_valid; k++)
+                        bulk_g2s(smem_addr(buf0 + static_cast<size_t>(k) * cf),
+                                 a.llr + static_cast<size_t>(cw0 + k) * n, cf * 4u, bar);
             }
             const long limit = a.wait_limit > 0 ? a.wait_limit : kWaitLimit;
             bool ok = mbar_wait_bounded(bar, phase, limit);
             if (!__syncthreads_and(ok)) {
+                // In a decode the copies read a valid device buffer and land
+                // (the wait only times out when they take longer than the
+                // limit); a second bounded wait gives them that time again
+                // before the CTA leaves, so no copy into this CTA's shared
+                // memory outlives it.  The self-test has none in flight.
                 if (tid == 0) atomicExch(a.error_flag, kErrLlrLoadTimeout);
-                mbar_wait_bounded(bar, phase, limit);  // let the copy in flight land before leaving
+                if (a.extra_tx == 0) mbar_wait_bounded(bar, phase, limit);
                 return;
             }
             phase ^= 1u;
@@ -722,6 +730,8 @@ __global__ void __launch_bounds__(kMaxThreads, 2)
         }
         bool ok = mbar_wait_bounded(bar, phase);
         if (!__syncthreads_and(ok)) {
+            // the copies read valid device buffers and land; a second bounded
+            // wait lets them do so before the CTA leaves (as decode_kernel)
             if (tid == 0) atomicExch(a.error_flag, kErrLlrLoadTimeout);
             mbar_wait_bounded(bar, phase);
             return;

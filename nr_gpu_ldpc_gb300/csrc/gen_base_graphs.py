@@ -61,7 +61,9 @@ def load_wifi_matrix(ref_root):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("NRLDPC_REF_ROOT")
+    if not ref_root:
+        raise SystemExit("usage: gen_base_graphs.py <reference tree> (or set NRLDPC_REF_ROOT)")
     graphs = {}
     for bg in (1, 2):
         tables = [load_nr_table(ref_root, bg, ils) for ils in range(8)]

@@ -13,17 +13,25 @@
 // Scratch: kNoAllocScratchBytes (96 MiB) for the check-node state of the
 // persistent decode CTAs, enough for two CTAs per SM of a 152-SM GB300 at the
 // largest code (BG1, Z = 384: 282,624 bytes per CTA), plus 256 bytes of
-// counters.  A GPU holds this memory from the first call of this entry point
-// on it (module load) until the process exits.
+// counters.  The array is reserved on a GPU when the CUDA runtime loads this
+// file's device module there, and held until the process exits: with lazy
+// module loading (CUDA's default) when a call of this file first touches the
+// array on that GPU (this entry point or nrldpc_noalloc_device_error); with
+// CUDA_MODULE_LOADING=EAGER at context creation, on every GPU the process
+// uses, whether or not it ever calls this entry point.
 //
-// Set-up: the first call on each device (the current device) looks up the
-// array's device address with cudaGetSymbolAddress and configures the
-// kernel's shared-memory limit; make that first call before any stream
-// capture.  All calls share the one array, which keeps the previous call's
-// contents: the scheduler counter is cleared on every call (the check-node
-// state is written before it is read), but calls that overlap on the GPU --
-// on different streams without ordering, or from several host threads --
-// race on the scratch and give wrong results.  Serialise them.
+// Set-up: the first successful call on each device (the current device)
+// looks up the array's device address with cudaGetSymbolAddress and
+// configures the kernel's shared-memory limit; make that first call before
+// any stream capture.  A set-up that fails is not remembered: the next call
+// tries again.  All calls share the one array, which keeps the previous
+// call's contents: the scheduler counter is cleared on every call (the
+// check-node state is written before it is read), but calls that overlap on
+// the GPU -- on different streams without ordering, or from several host
+// threads -- race on the scratch and give wrong results.  Serialise them.
+//
+// Errors found on the device (a bounded wait that ran out) are kept in the
+// array's error word until nrldpc_noalloc_device_error reads and clears it.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -43,7 +51,6 @@ static __device__ __align__(256) int g_noalloc_counters[64];  // [0] scheduler, 
 
 struct DeviceSetup {
     bool done;
-    int status;
     uint32_t* state;
     int* counters;
     int sm_count;
@@ -57,36 +64,31 @@ int setup_device(int dev, DeviceSetup** out) {
     std::lock_guard<std::mutex> lock(g_setup_mu);
     DeviceSetup& s = g_setup[dev];
     if (!s.done) {
-        s.done = true;
-        s.status = NRLDPC_OK;
         void* p = nullptr;
         void* q = nullptr;
         cudaDeviceProp prop;
         if (cudaGetSymbolAddress(&p, g_noalloc_state) != cudaSuccess ||
             cudaGetSymbolAddress(&q, g_noalloc_counters) != cudaSuccess ||
-            cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
-            s.status = NRLDPC_ERR_CUDA;
-        } else {
-            s.state = static_cast<uint32_t*>(p);
-            s.counters = static_cast<int*>(q);
-            s.sm_count = prop.multiProcessorCount;
-            s.smem_optin = prop.sharedMemPerBlockOptin;
-            s.smem_per_sm = prop.sharedMemPerMultiprocessor;
-            if (decode_kernel_attributes(s.smem_optin) != cudaSuccess) s.status = NRLDPC_ERR_CUDA;
+            cudaGetDeviceProperties(&prop, dev) != cudaSuccess ||
+            decode_kernel_attributes(prop.sharedMemPerBlockOptin) != cudaSuccess) {
+            cudaGetLastError();  // leave no sticky launch-side error behind; retried next call
+            return NRLDPC_ERR_CUDA;
         }
+        s.state = static_cast<uint32_t*>(p);
+        s.counters = static_cast<int*>(q);
+        s.sm_count = prop.multiProcessorCount;
+        s.smem_optin = prop.sharedMemPerBlockOptin;
+        s.smem_per_sm = prop.sharedMemPerMultiprocessor;
+        s.done = true;
     }
     *out = &s;
-    return s.status;
+    return NRLDPC_OK;
 }
 
-}  // namespace
-}  // namespace nrldpc
-
-using namespace nrldpc;
-
-extern "C" int nrldpc_decode_noalloc(int bg, int z, float alpha, const float* d_llr,
-                                     uint8_t* d_packed, int n_cw, int n_iter, int early_stop,
-                                     nrldpc_stream_t stream) {
+// Shared by the decode and its timeout self-test: wait_limit / extra_tx are
+// zero in every decode.
+int noalloc_decode(int bg, int z, float alpha, const float* d_llr, uint8_t* d_packed, int n_cw, int n_iter,
+                   int early_stop, cudaStream_t st, int wait_limit, uint32_t extra_tx) {
     if (n_cw < 0 || n_iter < 1 || (early_stop != 0 && early_stop != 1) || !(alpha > 0.0f))
         return NRLDPC_ERR_INVALID_ARG;
     CodeTable tab;
@@ -122,11 +124,46 @@ extern "C" int nrldpc_decode_noalloc(int bg, int z, float alpha, const float* d_
     a.n_groups = (n_cw + cpb - 1) / cpb;
     a.early_stop = early_stop;
     a.alpha = alpha;
+    a.wait_limit = wait_limit;
+    a.extra_tx = extra_tx;
     const long max_grid = std::min<long>(std::max(per_sm, 1) * static_cast<long>(s->sm_count),
                                          static_cast<long>(slots));
     const int grid = static_cast<int>(std::min<long>(a.n_groups, max_grid));
-    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    if (cudaMemsetAsync(s->counters, 0, 2 * sizeof(int), st) != cudaSuccess) return NRLDPC_ERR_CUDA;
+    // only the scheduler counter: the error word stays set until it is read
+    if (cudaMemsetAsync(s->counters, 0, sizeof(int), st) != cudaSuccess) return NRLDPC_ERR_CUDA;
     return launch_decode(tab, a, nullptr, grid, threads, smem, false, minb, st) == cudaSuccess ? NRLDPC_OK
                                                                                        : NRLDPC_ERR_CUDA;
+}
+
+}  // namespace
+}  // namespace nrldpc
+
+using namespace nrldpc;
+
+extern "C" int nrldpc_decode_noalloc(int bg, int z, float alpha, const float* d_llr,
+                                     uint8_t* d_packed, int n_cw, int n_iter, int early_stop,
+                                     nrldpc_stream_t stream) {
+    return noalloc_decode(bg, z, alpha, d_llr, d_packed, n_cw, n_iter, early_stop,
+                          reinterpret_cast<cudaStream_t>(stream), 0, 0);
+}
+
+// Reads the error word of the current device's static scratch with a
+// synchronous symbol copy (no allocation) and clears it when set.
+extern "C" int nrldpc_noalloc_device_error(void) {
+    int v = 0;
+    if (cudaMemcpyFromSymbol(&v, g_noalloc_counters, sizeof(int), sizeof(int)) != cudaSuccess)
+        return NRLDPC_ERR_CUDA;
+    if (v) {
+        const int zero = 0;
+        if (cudaMemcpyToSymbol(g_noalloc_counters, &zero, sizeof(int), sizeof(int)) != cudaSuccess)
+            return NRLDPC_ERR_CUDA;
+    }
+    return v ? NRLDPC_ERR_TIMEOUT : NRLDPC_OK;
+}
+
+extern "C" int nrldpc_selftest_noalloc_wait_timeout(int bg, int z, const float* d_llr, uint8_t* d_packed,
+                                                    int n_cw, nrldpc_stream_t stream) {
+    // 16 bytes expected and no copy issued, 1024 wait iterations
+    return noalloc_decode(bg, z, 0.75f, d_llr, d_packed, n_cw, 1, 0, reinterpret_cast<cudaStream_t>(stream),
+                          1024, 16);
 }

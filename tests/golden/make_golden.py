@@ -1,7 +1,8 @@
 """Generate the golden fixtures from the reference's own code.
 
 Runs only where the reference tree is present (it needs oracle/_ref, built by
-``make -C oracle REF=/root/reference``).  Every expected value below comes from
+``make -C oracle REF=<reference tree>``; the tree is taken from the first
+argument or NRLDPC_REF_ROOT, else the Makefile's default).  Every expected value below comes from
 the reference's source executed on the CPU:
 
 * decode results: src/ldpc_kernels.cu kernels replayed in the launch order of
@@ -82,7 +83,7 @@ def decode_case(name, code_kind, bg, z, ebn0, n_cw, iters_list, seed, full=False
 
 
 def main():
-    build("/root/reference")
+    build((sys.argv[1] if len(sys.argv) > 1 else None) or os.environ.get("NRLDPC_REF_ROOT") or None)
     for kind in ("bg1", "bg2", "wifi"):
         if not RefEmu.available(kind):
             raise SystemExit("oracle/_ref missing: the reference tree is required")

@@ -335,8 +335,8 @@ def test_every_lifting_size_against_oracle(gpu, bg):
 
 def test_bounded_wait_reports_timeout(gpu):
     """The wait for a group's LLR copy is bounded.  The self-test entry point
-    tells the copy barrier to expect 16 bytes more than the copies deliver,
-    so no CTA's wait can complete: each gives up after its limit, the kernel
+    tells the copy barrier to expect 16 bytes more than the copies deliver
+    and issues no copy, so no CTA's wait can complete: each gives up after its limit, the kernel
     records the timeout and returns, the host reads it (and reading clears
     it), and the same handle then decodes bit-exactly again."""
     lib = _lib.load()
