@@ -48,6 +48,7 @@ struct Handle {
     WeightTable* weights = nullptr;  // host copy, passed by value to the weighted kernels
     int n_w_iters = 0;
     bool wms_ready = false;
+    int wms_ctas = 1;  // training-kernel CTAs per SM (occupancy of the slowest of the four)
     int schedule = NRLDPC_SCHEDULE_FLOODING;
     int host_mode = NRLDPC_HOST_AUTO;
     bool coherent_host = false;  // the GPU reads host memory over a coherent link (Grace C2C)
@@ -596,13 +597,24 @@ namespace {
 struct WmsLayout {
     size_t states, gseed, gq, gh, total;
 };
+// Kernel attributes and CTAs per SM of the training kernels, once per handle.
+int wms_prepare(Handle* h) {
+    if (h->wms_ready) return NRLDPC_OK;
+    const size_t smem = wms_smem_bytes(h->tab, h->cpb);
+    if (cudaSetDevice(h->device) != cudaSuccess || wms_kernel_attributes(smem) != cudaSuccess)
+        return NRLDPC_ERR_CUDA;
+    h->wms_ctas = std::max(1, wms_ctas_per_sm(h->tab, h->threads, smem));
+    h->wms_ready = true;
+    return NRLDPC_OK;
+}
 // Workspace: per-iteration states and loss seeds, the flooding adjoint's
-// per-row dloss/dQ, and (layered schedule) the per-edge dloss/dR.
+// per-row dloss/dQ, and (layered schedule) the per-edge dloss/dR, the last
+// two per resident CTA slot.
 WmsLayout wms_layout(const Handle* h, int n_cw, int n_iter) {
     auto up = [](size_t x) { return (x + 255) / 256 * 256; };
     WmsLayout l;
     const size_t rz = static_cast<size_t>(h->tab.rows) * h->tab.z;
-    const size_t slots = static_cast<size_t>(h->sm_count) * h->cpb;
+    const size_t slots = static_cast<size_t>(h->sm_count) * h->wms_ctas * h->cpb;
     l.states = up(static_cast<size_t>(n_iter) * n_cw * rz * sizeof(uint4));
     l.gseed = up(static_cast<size_t>(n_iter) * n_cw * h->tab.n_bp * sizeof(float));
     l.gq = up(slots * rz * sizeof(uint4));
@@ -615,17 +627,15 @@ WmsLayout wms_layout(const Handle* h, int n_cw, int n_iter) {
 int wms_check(Handle* h, int n_cw, int n_iter) {
     if (!h || n_cw < 1 || n_iter < 1) return NRLDPC_ERR_INVALID_ARG;
     if (n_cw > h->max_batch) return NRLDPC_ERR_TOO_LARGE;
-    if (!h->wms_ready) {
-        if (wms_kernel_attributes(wms_smem_bytes(h->tab, h->cpb)) != cudaSuccess) return NRLDPC_ERR_CUDA;
-        h->wms_ready = true;
-    }
-    return NRLDPC_OK;
+    return wms_prepare(h);
 }
 }  // namespace
 
 int nrldpc_wms_workspace_bytes(nrldpc_handle* handle, int n_cw, int n_iter, size_t* bytes) {
     Handle* h = reinterpret_cast<Handle*>(handle);
     if (!h || !bytes || n_cw < 1 || n_iter < 1) return NRLDPC_ERR_INVALID_ARG;
+    const int rc = wms_prepare(h);
+    if (rc) return rc;
     *bytes = wms_layout(h, n_cw, n_iter).total;
     return NRLDPC_OK;
 }
@@ -648,7 +658,7 @@ int nrldpc_wms_forward(nrldpc_handle* handle, const float* d_llr, const uint8_t*
                                reinterpret_cast<uint4*>(ws + l.states + l.gseed),
                                lay ? reinterpret_cast<float*>(ws + l.states + l.gseed + l.gq) : nullptr,
                                d_loss, nullptr,
-                               d_app, h->scratch, n_cw, n_iter, h->cpb, h->sm_count, h->threads,
+                               d_app, h->scratch, n_cw, n_iter, h->cpb, h->sm_count * h->wms_ctas, h->threads,
                                wms_smem_bytes(h->tab, h->cpb), loss_scale, st));
 }
 
@@ -668,7 +678,7 @@ int nrldpc_wms_backward(nrldpc_handle* handle, int n_cw, int n_iter, const float
                                reinterpret_cast<uint4*>(ws + l.states + l.gseed),
                                lay ? reinterpret_cast<float*>(ws + l.states + l.gseed + l.gq) : nullptr,
                                nullptr, d_grad,
-                               nullptr, h->scratch, n_cw, n_iter, h->cpb, h->sm_count, h->threads,
+                               nullptr, h->scratch, n_cw, n_iter, h->cpb, h->sm_count * h->wms_ctas, h->threads,
                                wms_smem_bytes(h->tab, h->cpb), 0.0f, st));
 }
 

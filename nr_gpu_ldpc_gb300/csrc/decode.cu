@@ -304,6 +304,31 @@ __device__ __forceinline__ void write_outputs(const CodeTable& tab, const float*
                                               int bit, const uint4* st_slot, uint32_t s, uint8_t* packed,
                                               float* app, int32_t* iters, int it, bool app_from_state) {
     const int n = tab.n_bp, z = tab.z, ncz = tab.n_core * z;
+    if ((z & 31) == 0) {
+        // Warp ballots (the slot is whole warps): thread s decides positions
+        // s + k*Z (column k, sub-position s); one ballot over a warp is the
+        // 32 bits of positions 32*w .. 32*w + 31, LSB first = 4 packed bytes.
+        const uint32_t lane = s & 31u;
+        const bool word_store = (reinterpret_cast<uintptr_t>(packed) & 3u) == 0;
+        for (int k = 0, pos = static_cast<int>(s); pos < n; k++, pos += z) {
+            uint32_t one;
+            if (k < tab.n_core) {
+                one = L[pos] > 0.0f ? 0u : 1u;
+            } else {
+                const int r = tab.sfx_row[k];
+                int sr = static_cast<int>(s) - static_cast<int>(tab.edge_shift[tab.row_ptr[r + 1] - 1]);
+                if (sr < 0) sr += z;
+                one = (hd[r * z + sr] >> bit) & 1u;
+            }
+            const uint32_t word = __ballot_sync(0xffffffffu, one);
+            uint8_t* dst = packed + ((pos - static_cast<int>(lane)) >> 3);
+            if (word_store) {
+                if (lane == 0) *reinterpret_cast<uint32_t*>(dst) = word;
+            } else if (lane < 4) {
+                dst[lane] = static_cast<uint8_t>(word >> (8 * lane));
+            }
+        }
+    } else {
     for (int b = static_cast<int>(s); b < tab.packed_bytes; b += z) {
         int pos = 8 * b;
         int c = pos / z, p = pos - c * z;
@@ -325,6 +350,7 @@ __device__ __forceinline__ void write_outputs(const CodeTable& tab, const float*
             }
         }
         packed[b] = static_cast<uint8_t>(v);
+    }
     }
     if (app) {
         for (int pos = static_cast<int>(s); pos < ncz; pos += z) app[pos] = L[pos];

@@ -134,6 +134,7 @@ int decode_max_ctas_per_sm(bool weighted, int minb, int threads, size_t smem);
 // Learned weighted min-sum training kernels (wms.cu).
 size_t wms_smem_bytes(const CodeTable& tab, int cpb);
 cudaError_t wms_kernel_attributes(size_t smem);
+int wms_ctas_per_sm(const CodeTable& tab, int threads, size_t smem);
 cudaError_t launch_wms(bool backward, bool layered, const CodeTable& tab, const float* llr, const uint8_t* cw,
                        const float* weights, uint4* states, float* gseed, uint4* gq, float* gh, double* loss,
                        double* grad, float* app, int* counters, int n_cw, int T, int cpb, int grid,

@@ -43,24 +43,55 @@ __device__ __forceinline__ float max_nan(float a, float b) {
 
 __device__ __forceinline__ int cw_bit(const uint8_t* cw, int c) { return (cw[c >> 3] >> (c & 7)) & 1; }
 
+// Stored state of one lifted row after iteration t (16 B): min1, min2,
+// info = i1 | i2 << 5 | Q sign bits << 10 (i2 = 31: no second argmin), and
+// the posterior of the row's suffix column at this sub-row after the
+// iteration (unused in rows without one).  Suffix columns (degree 1, the last
+// edge of their row: 5G NR's extension parity) are touched by one row only,
+// so their posteriors and loss terms stay with that row's thread and only the
+// core columns live in shared memory.
+__device__ __forceinline__ uint32_t pack_info(int i1, int i2, uint32_t qmask) {
+    return static_cast<uint32_t>(i1) | (static_cast<uint32_t>(i2) << 5) | (qmask << 10);
+}
+
+// Position (c*Z + (s + V) mod Z) of sub-row s on edge word ed.
+__device__ __forceinline__ uint32_t edge_at(uint32_t ed, uint32_t s, uint32_t z) {
+    uint32_t a = s + (ed & 0xffffu);
+    if (s >= (ed >> 16)) a -= z;
+    return a;
+}
+
+// softplus(zz) = max(zz, 0) + log1p(e) and sigmoid(zz) = 1/(1 + e) (zz >= 0)
+// or e/(1 + e) (zz < 0), e = exp(-|zz|): one exponential per position.
+// Adds the position's loss to *loss and returns its gradient seed.
+__device__ __forceinline__ float loss_term(float L, bool bit1, float scale, float* loss) {
+    const float y = bit1 ? -1.0f : 1.0f;
+    const float zz = -y * L;
+    const float e = expf(-fabsf(zz));
+    *loss += fmaxf(zz, 0.0f) + log1pf(e);
+    const float r = __frcp_rn(1.0f + e);
+    return scale * (-y) * (zz >= 0.0f ? r : e * r);
+}
+
 // ---- forward ------------------------------------------------------------------------
+// sfx: the row's last edge is a suffix column, its posterior is st.w (read)
+// and the stored state's w (written); its loss term and seed are taken here.
 template <int D, bool LAYERED>
 __device__ __forceinline__ void fwd_row(const CodeTable& tab, int e0, uint32_t s, const float* lold,
                                         float* lnew, const float* w_prev, const float* w_cur,
-                                        uint4 st, uint4* st_out) {
+                                        uint4 st, uint4* st_out, bool sfx, bool ybit, float* seed_t,
+                                        float scale, float* loss) {
+    constexpr int LAST = D - 1;
     const uint32_t z = static_cast<uint32_t>(tab.z);
     uint32_t addr[D];
     float lv[D], rold[D];
 #pragma unroll
     for (int i = 0; i < D; i++) {
-        const uint32_t ed = tab.edge[e0 + i];
-        uint32_t a = s + (ed & 0xffffu);
-        if (s >= (ed >> 16)) a -= z;
-        addr[i] = a;
-        lv[i] = lold[a];
+        addr[i] = edge_at(tab.edge[e0 + i], s, z);
+        lv[i] = (i == LAST && sfx) ? __uint_as_float(st.w) : lold[addr[i]];
     }
     const float om1 = __uint_as_float(st.x), om2 = __uint_as_float(st.y);
-    const uint32_t oq = st.z >> 8;
+    const uint32_t oq = st.z >> 10;
     const int oidx = static_cast<int>(st.z & 31u);
     const uint32_t opar = static_cast<uint32_t>(__popc(oq) & 1);
     float m1 = 1000.0f, m2 = 1000.0f;
@@ -85,36 +116,46 @@ __device__ __forceinline__ void fwd_row(const CodeTable& tab, int e0, uint32_t s
     const uint32_t par = static_cast<uint32_t>(__popc(qmask) & 1);
     float nv[D];
 #pragma unroll
-    for (int i = 0; i < D; i++) nv[i] = LAYERED ? 0.0f : lnew[addr[i]];
+    for (int i = 0; i < D; i++) nv[i] = (LAYERED || (i == LAST && sfx)) ? lv[i] : lnew[addr[i]];
+    float sfx_new = 0.0f;
 #pragma unroll
     for (int i = 0; i < D; i++) {
         const float mag = __fmul_rn(w_cur[e0 + i], i == i1 ? m2 : m1);
         const uint32_t sb = (par ^ (qmask >> i)) & 1u;
         const float rn = __uint_as_float(__float_as_uint(mag) ^ (sb << 31));
-        if (LAYERED)
-            lnew[addr[i]] = __fadd_rn(rold[i], rn);  // A = Q + R_new
+        // layered: A = Q + R_new; flooding: Lnew += R_new - R_old
+        const float v = LAYERED ? __fadd_rn(rold[i], rn) : __fadd_rn(nv[i], __fsub_rn(rn, rold[i]));
+        if (i == LAST && sfx)
+            sfx_new = v;
         else
-            lnew[addr[i]] = __fadd_rn(nv[i], __fsub_rn(rn, rold[i]));
+            lnew[addr[i]] = v;
     }
-    *st_out = make_uint4(__float_as_uint(m1), __float_as_uint(m2),
-                         static_cast<uint32_t>(i1) | (qmask << 8), static_cast<uint32_t>(i2));
+    *st_out = make_uint4(__float_as_uint(m1), __float_as_uint(m2), pack_info(i1, i2, qmask),
+                         __float_as_uint(sfx_new));
+    if (sfx) seed_t[addr[LAST]] = loss_term(sfx_new, ybit, scale, loss);
 }
 
-template <bool LAYERED>
+// Degree switch up to MAXD (the code's largest row degree class: 10 covers
+// BG2, 19 BG1), so a BG2 kernel holds no registers for BG1's long rows.
+#define NRLDPC_DEG_SWITCH(CASE)                                                                  \
+    switch (deg) {                                                                               \
+        CASE(1) CASE(2) CASE(3) CASE(4) CASE(5) CASE(6) CASE(7) CASE(8) CASE(9) CASE(10)        \
+        CASE(11) CASE(12) CASE(13) CASE(14) CASE(15) CASE(16) CASE(17) CASE(18) CASE(19)        \
+        default: break;                                                                          \
+    }
+
+template <int MAXD, bool LAYERED>
 __device__ __forceinline__ void fwd_dispatch(int deg, const CodeTable& tab, int e0, uint32_t s,
                                              const float* lold, float* lnew, const float* wp,
-                                             const float* wc, uint4 st, uint4* st_out) {
-    switch (deg) {
-#define NRLDPC_FWD_CASE(D) \
-    case D: fwd_row<D, LAYERED>(tab, e0, s, lold, lnew, wp, wc, st, st_out); break;
-        NRLDPC_FWD_CASE(1) NRLDPC_FWD_CASE(2) NRLDPC_FWD_CASE(3) NRLDPC_FWD_CASE(4)
-        NRLDPC_FWD_CASE(5) NRLDPC_FWD_CASE(6) NRLDPC_FWD_CASE(7) NRLDPC_FWD_CASE(8)
-        NRLDPC_FWD_CASE(9) NRLDPC_FWD_CASE(10) NRLDPC_FWD_CASE(11) NRLDPC_FWD_CASE(12)
-        NRLDPC_FWD_CASE(13) NRLDPC_FWD_CASE(14) NRLDPC_FWD_CASE(15) NRLDPC_FWD_CASE(16)
-        NRLDPC_FWD_CASE(17) NRLDPC_FWD_CASE(18) NRLDPC_FWD_CASE(19)
+                                             const float* wc, uint4 st, uint4* st_out, bool sfx, bool ybit,
+                                             float* seed_t, float scale, float* loss) {
+#define NRLDPC_FWD_CASE(D)                                                                         \
+    case D:                                                                                        \
+        if constexpr (D <= MAXD)                                                                   \
+            fwd_row<D, LAYERED>(tab, e0, s, lold, lnew, wp, wc, st, st_out, sfx, ybit, seed_t, scale, loss); \
+        break;
+    NRLDPC_DEG_SWITCH(NRLDPC_FWD_CASE)
 #undef NRLDPC_FWD_CASE
-        default: break;
-    }
 }
 
 struct WmsArgs {
@@ -134,8 +175,12 @@ struct WmsArgs {
     float scale;
 };
 
-template <bool LAYERED>
-__global__ void __launch_bounds__(kMaxThreads, 1)
+// Two CTAs per SM: registers are capped for it (the BG1 kernels spill a
+// little at degree 19, the BG2 ones do not).
+constexpr int kWmsMinBlocks = 2;
+
+template <int MAXD, bool LAYERED>
+__global__ void __launch_bounds__(kMaxThreads, kWmsMinBlocks)
     wms_forward_kernel(const __grid_constant__ CodeTable tab, const __grid_constant__ WmsArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     int* s_group = reinterpret_cast<int*>(smem);
@@ -143,6 +188,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
     float* wbuf = reinterpret_cast<float*>(smem + kHdr);  // [2][E] previous / current weights
     float* bufs = wbuf + 2 * kMaxEdges;
     const int z = tab.z, n = tab.n_bp, cpb = a.cpb, rows = tab.rows, E = tab.n_edges;
+    const int cf = tab.core_floats, ncz = tab.n_core * z;
     const int tid = threadIdx.x, slot = tid / z;
     const uint32_t s = static_cast<uint32_t>(tid - slot * z);
     const bool valid = slot < cpb;
@@ -153,24 +199,30 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
         if (g >= a.n_groups) break;
         const int cw = g * cpb + slot;
         const bool act = valid && cw < a.n_cw;
-        float* lold = bufs + static_cast<size_t>(slot) * n;
-        float* lnew = LAYERED ? lold : bufs + static_cast<size_t>(cpb + slot) * n;
-        // this thread's codeword bits at positions s, s + Z, s + 2Z, ... (at
-        // most kMaxCols of them) as a 128-bit mask, read once per group
-        uint64_t ybits0 = 0, ybits1 = 0;
+        float* lold = bufs + static_cast<size_t>(valid ? slot : 0) * cf;
+        float* lnew = LAYERED ? lold : bufs + static_cast<size_t>(cpb + (valid ? slot : 0)) * cf;
+        const float* gllr = a.llr + static_cast<size_t>(act ? cw : 0) * n;
+        // this thread's codeword bits: core positions s, s + Z, ... (at most
+        // kMaxCols) as a 128-bit mask, and bit r = the bit at row r's suffix
+        // position of sub-row s; read once per group
+        uint64_t ybits0 = 0, ybits1 = 0, ysfx = 0;
         if (act) {
-            const float4* src = reinterpret_cast<const float4*>(a.llr + static_cast<size_t>(cw) * n);
 #pragma unroll 4
-            for (int k = static_cast<int>(s); k < n / 4; k += z) reinterpret_cast<float4*>(lold)[k] = src[k];
+            for (int k = static_cast<int>(s); k < cf / 4; k += z)
+                reinterpret_cast<float4*>(lold)[k] = reinterpret_cast<const float4*>(gllr)[k];
             const uint8_t* bits = a.cw + static_cast<size_t>(cw) * tab.packed_bytes;
-#pragma unroll 4
-            for (int k = 0; k < tab.cols; k++) {
+            for (int k = 0; k < tab.n_core; k++) {
                 const uint64_t b = static_cast<uint64_t>(cw_bit(bits, static_cast<int>(s) + k * z));
                 if (k < 64)
                     ybits0 |= b << k;
                 else
                     ybits1 |= b << (k - 64);
             }
+            for (int r = 0; r < rows; r++)
+                if (tab.row_sfx[r])
+                    ysfx |= static_cast<uint64_t>(
+                                cw_bit(bits, static_cast<int>(edge_at(tab.edge[tab.row_ptr[r + 1] - 1], s, z))))
+                            << r;
         }
         float loss_part = 0.0f;
         for (int t = 0; t < a.T; t++) {
@@ -180,52 +232,58 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
             }
             __syncthreads();
             if (act && !LAYERED)
-                for (int k = static_cast<int>(s); k < n / 4; k += z)
+                for (int k = static_cast<int>(s); k < cf / 4; k += z)
                     reinterpret_cast<float4*>(lnew)[k] = reinterpret_cast<const float4*>(lold)[k];
             __syncthreads();
             const size_t cw_off = static_cast<size_t>(act ? cw : 0) * rows * z;
             const uint4* st_prev =
                 a.states + static_cast<size_t>(t > 0 ? t - 1 : 0) * a.n_cw * rows * z + cw_off;
             uint4* st_cur = a.states + static_cast<size_t>(t) * a.n_cw * rows * z + cw_off;
-            // previous iteration's state of row r+2 requested while row r runs
+            float* seed_t = a.gseed + (static_cast<size_t>(t) * a.n_cw + (act ? cw : 0)) * n;
+            // previous iteration's state of row r+2 requested while row r
+            // runs; in the first iteration only the suffix LLR, from global
             auto fetch = [&](int r) -> uint4 {
-                return (act && t > 0 && r < rows) ? __ldcg(st_prev + r * z + s) : make_uint4(0u, 0u, 0u, 0u);
+                uint4 v = make_uint4(0u, 0u, 0u, 0u);
+                if (!act || r >= rows) return v;
+                if (t > 0) return __ldcg(st_prev + r * z + s);
+                if (tab.row_sfx[r])
+                    v.w = __float_as_uint(__ldcs(gllr + edge_at(tab.edge[tab.row_ptr[r + 1] - 1], s, z)));
+                return v;
             };
             uint4 p0 = fetch(0), p1 = fetch(1);
             for (int r = 0; r < rows; r++) {
                 const uint4 p2 = fetch(r + 2);
                 if (act)
-                    fwd_dispatch<LAYERED>(tab.row_deg[r], tab, tab.row_ptr[r], s, lold, lnew, wbuf,
-                                          wbuf + kMaxEdges, p0, st_cur + r * z + s);
+                    fwd_dispatch<MAXD, LAYERED>(tab.row_deg[r], tab, tab.row_ptr[r], s, lold, lnew, wbuf,
+                                                wbuf + kMaxEdges, p0, st_cur + r * z + s, tab.row_sfx[r] != 0,
+                                                (ysfx >> r) & 1u, seed_t, a.scale, &loss_part);
                 p0 = p1;
                 p1 = p2;
                 if (tab.sync_after[r]) __syncthreads();
             }
-            // loss term and its gradient seed at L^{t+1}
+            // loss terms and gradient seeds of the core columns at L^{t+1}
             if (act) {
-                float* seed = a.gseed + (static_cast<size_t>(t) * a.n_cw + cw) * n;
                 uint64_t y0 = ybits0, y1 = ybits1;
-                // softplus(zz) = max(zz, 0) + log1p(e) and sigmoid(zz) =
-                // 1/(1 + e) (zz >= 0) or e/(1 + e) (zz < 0), e = exp(-|zz|):
-                // one exponential per position
 #pragma unroll 4
-                for (int c = static_cast<int>(s); c < n; c += z) {
-                    const float y = (y0 & 1u) ? -1.0f : 1.0f;
+                for (int c = static_cast<int>(s); c < ncz; c += z) {
+                    seed_t[c] = loss_term(lnew[c], y0 & 1u, a.scale, &loss_part);
                     y0 = (y0 >> 1) | (y1 << 63);
                     y1 >>= 1;
-                    const float zz = -y * lnew[c];
-                    const float e = expf(-fabsf(zz));
-                    loss_part += fmaxf(zz, 0.0f) + log1pf(e);
-                    const float r = __frcp_rn(1.0f + e);
-                    seed[c] = a.scale * (-y) * (zz >= 0.0f ? r : e * r);
                 }
             }
             float* tmp = lold;
             lold = lnew;
             lnew = tmp;
         }
-        if (act && a.app)
-            for (int c = static_cast<int>(s); c < n; c += z) a.app[static_cast<size_t>(cw) * n + c] = lold[c];
+        if (act && a.app) {
+            float* app = a.app + static_cast<size_t>(cw) * n;
+            for (int c = static_cast<int>(s); c < ncz; c += z) app[c] = lold[c];
+            const uint4* st_last = a.states + (static_cast<size_t>(a.T - 1) * a.n_cw + cw) * rows * z;
+            for (int r = 0; r < rows; r++)
+                if (tab.row_sfx[r])
+                    app[edge_at(tab.edge[tab.row_ptr[r + 1] - 1], s, z)] =
+                        __uint_as_float(__ldcg(&st_last[r * z + s].w));
+        }
         // block reduction of the loss
         for (int off = 16; off > 0; off >>= 1) loss_part += __shfl_xor_sync(0xffffffffu, loss_part, off);
         if ((tid & 31) == 0) s_red[tid >> 5] = loss_part;
@@ -275,14 +333,19 @@ __device__ __forceinline__ void warp_sum_to(float (&v)[D], float* acc) {
 }
 
 // ---- adjoint ------------------------------------------------------------------------
+// gl = dloss/dL^{t+1} and gl_next = dloss/dL^t over the core columns.  The
+// suffix edge's dloss/dL^{t+1} is its loss seed plus what the next
+// iteration's row sent back through Q (only this row touches the column).
 template <int D>
 __device__ __forceinline__ void bwd_row(const CodeTable& tab, int e0, uint32_t s, bool act,
                                         const float* gl, float* gl_next, const float* w_cur,
-                                        float* gw_acc, uint4 st, uint4 gin, uint4* gq_io, bool scatter) {
+                                        float* gw_acc, uint4 st, uint4 gin, uint4* gq_io, bool scatter,
+                                        bool sfx, float sfx_seed) {
+    constexpr int LAST = D - 1;
     const uint32_t z = static_cast<uint32_t>(tab.z);
     const float m1 = __uint_as_float(st.x), m2 = __uint_as_float(st.y);
-    const int i1 = static_cast<int>(st.z & 31u), i2 = static_cast<int>(st.w);
-    const uint32_t q = st.z >> 8;
+    const int i1 = static_cast<int>(st.z & 31u), i2 = static_cast<int>((st.z >> 5) & 31u);
+    const uint32_t q = st.z >> 10;
     const uint32_t par = static_cast<uint32_t>(__popc(q) & 1);
     const float g1n = __uint_as_float(gin.x), g2n = __uint_as_float(gin.y);
     const int j1 = static_cast<int>(gin.z), j2 = static_cast<int>(gin.w);
@@ -291,13 +354,15 @@ __device__ __forceinline__ void bwd_row(const CodeTable& tab, int e0, uint32_t s
     float gwv[D];
 #pragma unroll
     for (int i = 0; i < D; i++) {
-        const uint32_t ed = tab.edge[e0 + i];
-        uint32_t a = s + (ed & 0xffffu);
-        if (s >= (ed >> 16)) a -= z;
+        const uint32_t a = edge_at(tab.edge[e0 + i], s, z);
         ad1 = i == i1 ? a : ad1;
         ad2 = i == i2 ? a : ad2;
         float gr = 0.0f;
-        if (act) gr = gl[a] - (i == j1 ? g1n : (i == j2 ? g2n : 0.0f));
+        if (act) {
+            const float back = i == j1 ? g1n : (i == j2 ? g2n : 0.0f);
+            const float glv = (i == LAST && sfx) ? __fadd_rn(sfx_seed, back) : gl[a];
+            gr = glv - back;
+        }
         const float sg = ((par ^ (q >> i)) & 1u) ? -1.0f : 1.0f;
         const float mag = i == i1 ? m2 : m1;
         gwv[i] = act ? gr * sg * mag : 0.0f;
@@ -310,32 +375,30 @@ __device__ __forceinline__ void bwd_row(const CodeTable& tab, int e0, uint32_t s
     if (act) {
         if (m1 < 1000.0f) g1 = acc1 * (((q >> i1) & 1u) ? -1.0f : 1.0f);
         if (i2 < D && m2 < 1000.0f) g2 = acc2 * (((q >> i2) & 1u) ? -1.0f : 1.0f);
-        if (scatter) {
-            if (m1 < 1000.0f) atomicAdd(&gl_next[ad1], g1);
-            if (i2 < D && m2 < 1000.0f) atomicAdd(&gl_next[ad2], g2);
+        if (scatter) {  // the suffix column's share comes back through gq instead
+            if (m1 < 1000.0f && !(sfx && i1 == LAST)) atomicAdd(&gl_next[ad1], g1);
+            if (i2 < D && m2 < 1000.0f && !(sfx && i2 == LAST)) atomicAdd(&gl_next[ad2], g2);
         }
         *gq_io = make_uint4(__float_as_uint(g1), __float_as_uint(g2), static_cast<uint32_t>(i1),
                             static_cast<uint32_t>(i2 < D ? i2 : 31));
     }
 }
 
+template <int MAXD>
 __device__ __forceinline__ void bwd_dispatch(int deg, const CodeTable& tab, int e0, uint32_t s,
                                              bool act, const float* gl, float* gln, const float* wc,
-                                             float* gw_acc, uint4 st, uint4 gin, uint4* gq, bool scatter) {
-    switch (deg) {
-#define NRLDPC_BWD_CASE(D) \
-    case D: bwd_row<D>(tab, e0, s, act, gl, gln, wc, gw_acc, st, gin, gq, scatter); break;
-        NRLDPC_BWD_CASE(1) NRLDPC_BWD_CASE(2) NRLDPC_BWD_CASE(3) NRLDPC_BWD_CASE(4)
-        NRLDPC_BWD_CASE(5) NRLDPC_BWD_CASE(6) NRLDPC_BWD_CASE(7) NRLDPC_BWD_CASE(8)
-        NRLDPC_BWD_CASE(9) NRLDPC_BWD_CASE(10) NRLDPC_BWD_CASE(11) NRLDPC_BWD_CASE(12)
-        NRLDPC_BWD_CASE(13) NRLDPC_BWD_CASE(14) NRLDPC_BWD_CASE(15) NRLDPC_BWD_CASE(16)
-        NRLDPC_BWD_CASE(17) NRLDPC_BWD_CASE(18) NRLDPC_BWD_CASE(19)
+                                             float* gw_acc, uint4 st, uint4 gin, uint4* gq, bool scatter,
+                                             bool sfx, float sfx_seed) {
+#define NRLDPC_BWD_CASE(D)                                                                           \
+    case D:                                                                                          \
+        if constexpr (D <= MAXD) bwd_row<D>(tab, e0, s, act, gl, gln, wc, gw_acc, st, gin, gq, scatter, sfx, sfx_seed); \
+        break;
+    NRLDPC_DEG_SWITCH(NRLDPC_BWD_CASE)
 #undef NRLDPC_BWD_CASE
-        default: break;
-    }
 }
 
-__global__ void __launch_bounds__(kMaxThreads, 1)
+template <int MAXD>
+__global__ void __launch_bounds__(kMaxThreads, kWmsMinBlocks)
     wms_backward_kernel(const __grid_constant__ CodeTable tab, const __grid_constant__ WmsArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     int* s_group = reinterpret_cast<int*>(smem);
@@ -343,6 +406,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
     float* gw_acc = wcur + kMaxEdges;                     // [E]
     float* bufs = gw_acc + kMaxEdges;
     const int z = tab.z, n = tab.n_bp, cpb = a.cpb, rows = tab.rows, E = tab.n_edges;
+    const int cf = tab.core_floats, ncz = tab.n_core * z;
     const int tid = threadIdx.x, slot = tid / z;
     const uint32_t s = static_cast<uint32_t>(tid - slot * z);
     const bool valid = slot < cpb;
@@ -354,12 +418,12 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
         if (g >= a.n_groups) break;
         const int cw = g * cpb + slot;
         const bool act = valid && cw < a.n_cw;
-        float* gl = bufs + static_cast<size_t>(slot) * n;           // dloss/dL^{t+1}
-        float* gln = bufs + static_cast<size_t>(cpb + slot) * n;    // dloss/dL^t
+        float* gl = bufs + static_cast<size_t>(valid ? slot : 0) * cf;          // dloss/dL^{t+1}
+        float* gln = bufs + static_cast<size_t>(cpb + (valid ? slot : 0)) * cf;  // dloss/dL^t
         if (act) {
             const float* seed = a.gseed + (static_cast<size_t>(a.T - 1) * a.n_cw + cw) * n;
 #pragma unroll 4
-            for (int c = static_cast<int>(s); c < n; c += z) gl[c] = seed[c];
+            for (int c = static_cast<int>(s); c < ncz; c += z) gl[c] = seed[c];
             for (int k = 0; k < rows; k++) gq[k * z + s] = make_uint4(0u, 0u, 31u, 31u);
         }
         for (int t = a.T - 1; t >= 0; t--) {
@@ -367,36 +431,42 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
                 wcur[e] = a.weights[t * E + e];
                 gw_acc[e] = 0.0f;
             }
-            if (act) {
-                if (t > 0) {
-                    const float* seed = a.gseed + (static_cast<size_t>(t - 1) * a.n_cw + cw) * n;
+            if (act && t > 0) {
+                const float* seed = a.gseed + (static_cast<size_t>(t - 1) * a.n_cw + cw) * n;
 #pragma unroll 4
-                    for (int c = static_cast<int>(s); c < n; c += z) gln[c] = seed[c];
-                }
+                for (int c = static_cast<int>(s); c < ncz; c += z) gln[c] = seed[c];
             }
             __syncthreads();
             const uint4* st = a.states + (static_cast<size_t>(t) * a.n_cw + (act ? cw : 0)) * rows * z;
-            // state and per-row dloss/dQ of row r+2 requested while row r runs
-            auto fetch = [&](int r, uint4& sv, uint4& gv) {
-                sv = make_uint4(0u, 0u, 0u, 31u);
+            const float* seed_t = a.gseed + (static_cast<size_t>(t) * a.n_cw + (act ? cw : 0)) * n;
+            // state, per-row dloss/dQ and the suffix edge's loss seed of row
+            // r+2 requested while row r runs
+            auto fetch = [&](int r, uint4& sv, uint4& gv, float& sd) {
+                sv = make_uint4(0u, 0u, 31u << 5, 0u);
                 gv = make_uint4(0u, 0u, 31u, 31u);
+                sd = 0.0f;
                 if (act && r < rows) {
                     sv = __ldcg(st + r * z + s);
                     gv = __ldcg(gq + r * z + s);
+                    if (tab.row_sfx[r]) sd = __ldcs(seed_t + edge_at(tab.edge[tab.row_ptr[r + 1] - 1], s, z));
                 }
             };
             uint4 s0, g0, s1, g1;
-            fetch(0, s0, g0);
-            fetch(1, s1, g1);
+            float d0, d1;
+            fetch(0, s0, g0, d0);
+            fetch(1, s1, g1, d1);
             for (int r = 0; r < rows; r++) {
                 uint4 s2, g2;
-                fetch(r + 2, s2, g2);
-                bwd_dispatch(tab.row_deg[r], tab, tab.row_ptr[r], s, act, gl, gln, wcur, gw_acc, s0, g0,
-                             gq + r * z + s, t > 0);
+                float d2;
+                fetch(r + 2, s2, g2, d2);
+                bwd_dispatch<MAXD>(tab.row_deg[r], tab, tab.row_ptr[r], s, act, gl, gln, wcur, gw_acc, s0, g0,
+                                   gq + r * z + s, t > 0, tab.row_sfx[r] != 0, d0);
                 s0 = s1;
                 g0 = g1;
+                d0 = d1;
                 s1 = s2;
                 g1 = g2;
+                d1 = d2;
             }
             __syncthreads();
             for (int e = tid; e < E; e += blockDim.x)
@@ -409,14 +479,19 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
     }
 }
 
-template <int D>
+// g = dloss/dA over the core columns.  The suffix column's dloss/dA before
+// its row is its loss seed minus the dloss/dR carried from the next
+// iteration (h = -dloss/dQ there), the value the in-place A had.
+template <int D, bool SEED_IN_ROW>
 __device__ __forceinline__ void bwd_layered_row(const CodeTable& tab, int e0, uint32_t s, bool act, float* g,
                                                 const float* w_cur, float* gw_acc, uint4 st, float* gh_row,
-                                                bool has_h, bool write_h) {
+                                                bool has_h, bool write_h, bool sfx, float sfx_seed,
+                                                const float* seed_t) {
+    constexpr int LAST = D - 1;
     const uint32_t z = static_cast<uint32_t>(tab.z);
     const float m1 = __uint_as_float(st.x), m2 = __uint_as_float(st.y);
-    const int i1 = static_cast<int>(st.z & 31u), i2 = static_cast<int>(st.w);
-    const uint32_t q = st.z >> 8;
+    const int i1 = static_cast<int>(st.z & 31u), i2 = static_cast<int>((st.z >> 5) & 31u);
+    const uint32_t q = st.z >> 10;
     const uint32_t par = static_cast<uint32_t>(__popc(q) & 1);
     uint32_t ad[D];
     float ga[D];
@@ -424,15 +499,14 @@ __device__ __forceinline__ void bwd_layered_row(const CodeTable& tab, int e0, ui
     float to1 = 0.0f, to2 = 0.0f;  // dloss/dQ at the argmin edges through R
 #pragma unroll
     for (int i = 0; i < D; i++) {
-        const uint32_t ed = tab.edge[e0 + i];
-        uint32_t a = s + (ed & 0xffffu);
-        if (s >= (ed >> 16)) a -= z;
+        const uint32_t a = edge_at(tab.edge[e0 + i], s, z);
         ad[i] = a;
         float dr = 0.0f;
         ga[i] = 0.0f;
         if (act) {
-            ga[i] = g[a];
-            dr = ga[i] + (has_h ? gh_row[i * z] : 0.0f);
+            const float h = has_h ? gh_row[i * z] : 0.0f;
+            ga[i] = (i == LAST && sfx) ? __fsub_rn(SEED_IN_ROW ? __ldcs(seed_t + a) : sfx_seed, h) : g[a];
+            dr = ga[i] + h;
         }
         const float sg = ((par ^ (q >> i)) & 1u) ? -1.0f : 1.0f;
         const float mag = i == i1 ? m2 : m1;
@@ -450,28 +524,28 @@ __device__ __forceinline__ void bwd_layered_row(const CodeTable& tab, int e0, ui
         float dq = ga[i];
         if (i == i1) dq += g1;
         if (i == i2) dq += g2;
-        if (i == i1 || i == i2) g[ad[i]] = dq;  // dloss/dA before this row
-        if (write_h) gh_row[i * z] = -dq;      // dloss/dR^{t-1}
+        if ((i == i1 || i == i2) && !(i == LAST && sfx)) g[ad[i]] = dq;  // dloss/dA before this row
+        if (write_h) gh_row[i * z] = -dq;                                // dloss/dR^{t-1}
     }
 }
 
+template <int MAXD>
 __device__ __forceinline__ void bwd_layered_dispatch(int deg, const CodeTable& tab, int e0, uint32_t s, bool act,
                                                      float* g, const float* wc, float* gw_acc, uint4 st,
-                                                     float* gh_row, bool has_h, bool write_h) {
-    switch (deg) {
-#define NRLDPC_BWDL_CASE(D) \
-    case D: bwd_layered_row<D>(tab, e0, s, act, g, wc, gw_acc, st, gh_row, has_h, write_h); break;
-        NRLDPC_BWDL_CASE(1) NRLDPC_BWDL_CASE(2) NRLDPC_BWDL_CASE(3) NRLDPC_BWDL_CASE(4)
-        NRLDPC_BWDL_CASE(5) NRLDPC_BWDL_CASE(6) NRLDPC_BWDL_CASE(7) NRLDPC_BWDL_CASE(8)
-        NRLDPC_BWDL_CASE(9) NRLDPC_BWDL_CASE(10) NRLDPC_BWDL_CASE(11) NRLDPC_BWDL_CASE(12)
-        NRLDPC_BWDL_CASE(13) NRLDPC_BWDL_CASE(14) NRLDPC_BWDL_CASE(15) NRLDPC_BWDL_CASE(16)
-        NRLDPC_BWDL_CASE(17) NRLDPC_BWDL_CASE(18) NRLDPC_BWDL_CASE(19)
+                                                     float* gh_row, bool has_h, bool write_h, bool sfx,
+                                                     float sfx_seed, const float* seed_t) {
+#define NRLDPC_BWDL_CASE(D)                                                                                 \
+    case D:                                                                                                 \
+        if constexpr (D <= MAXD)                                                                            \
+            bwd_layered_row<D, (MAXD > 10)>(tab, e0, s, act, g, wc, gw_acc, st, gh_row, has_h, write_h, sfx,      \
+                                            sfx_seed, seed_t);                                                    \
+        break;
+    NRLDPC_DEG_SWITCH(NRLDPC_BWDL_CASE)
 #undef NRLDPC_BWDL_CASE
-        default: break;
-    }
 }
 
-__global__ void __launch_bounds__(kMaxThreads, 1)
+template <int MAXD>
+__global__ void __launch_bounds__(kMaxThreads, kWmsMinBlocks)
     wms_backward_layered_kernel(const __grid_constant__ CodeTable tab, const __grid_constant__ WmsArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     int* s_group = reinterpret_cast<int*>(smem);
@@ -479,6 +553,7 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
     float* gw_acc = wcur + kMaxEdges;                     // [E]
     float* bufs = gw_acc + kMaxEdges;
     const int z = tab.z, n = tab.n_bp, cpb = a.cpb, rows = tab.rows, E = tab.n_edges;
+    const int cf = tab.core_floats, ncz = tab.n_core * z;
     const int tid = threadIdx.x, slot = tid / z;
     const uint32_t s = static_cast<uint32_t>(tid - slot * z);
     const bool valid = slot < cpb;
@@ -490,31 +565,43 @@ __global__ void __launch_bounds__(kMaxThreads, 1)
         if (grp >= a.n_groups) break;
         const int cw = grp * cpb + slot;
         const bool act = valid && cw < a.n_cw;
-        float* g = bufs + static_cast<size_t>(valid ? slot : 0) * n;  // dloss/dA
+        float* g = bufs + static_cast<size_t>(valid ? slot : 0) * cf;  // dloss/dA
         if (act)
-            for (int c = static_cast<int>(s); c < n; c += z) g[c] = 0.0f;
+            for (int c = static_cast<int>(s); c < ncz; c += z) g[c] = 0.0f;
         for (int t = a.T - 1; t >= 0; t--) {
             for (int e = tid; e < E; e += blockDim.x) {
                 wcur[e] = a.weights[t * E + e];
                 gw_acc[e] = 0.0f;
             }
+            const float* seed_t = a.gseed + (static_cast<size_t>(t) * a.n_cw + (act ? cw : 0)) * n;
             if (act) {
-                const float* seed = a.gseed + (static_cast<size_t>(t) * a.n_cw + cw) * n;
 #pragma unroll 4
-                for (int c = static_cast<int>(s); c < n; c += z) g[c] += seed[c];
+                for (int c = static_cast<int>(s); c < ncz; c += z) g[c] += seed_t[c];
             }
             __syncthreads();
             const uint4* st = a.states + (static_cast<size_t>(t) * a.n_cw + (act ? cw : 0)) * rows * z;
-            auto fetch = [&](int r) -> uint4 {  // state of row r-2 requested while row r runs
-                return (act && r >= 0) ? __ldcg(st + r * z + s) : make_uint4(0u, 0u, 0u, 31u);
+            // state of row r-2 requested while row r runs, with its suffix
+            // loss seed in the degree-10 kernels (at degree 19 the extra
+            // registers of the seed ring cost more in spills than it saves)
+            auto fetch = [&](int r, float& sd) -> uint4 {
+                sd = 0.0f;
+                if (!act || r < 0) return make_uint4(0u, 0u, 31u << 5, 0u);
+                if (MAXD <= 10 && tab.row_sfx[r])
+                    sd = __ldcs(seed_t + edge_at(tab.edge[tab.row_ptr[r + 1] - 1], s, z));
+                return __ldcg(st + r * z + s);
             };
-            uint4 s0 = fetch(rows - 1), s1 = fetch(rows - 2);
+            float d0, d1;
+            uint4 s0 = fetch(rows - 1, d0), s1 = fetch(rows - 2, d1);
             for (int r = rows - 1; r >= 0; r--) {
-                const uint4 s2 = fetch(r - 2);
-                bwd_layered_dispatch(tab.row_deg[r], tab, tab.row_ptr[r], s, act, g, wcur, gw_acc, s0,
-                                     gh + static_cast<size_t>(tab.row_ptr[r]) * z + s, t < a.T - 1, t > 0);
+                float d2;
+                const uint4 s2 = fetch(r - 2, d2);
+                bwd_layered_dispatch<MAXD>(tab.row_deg[r], tab, tab.row_ptr[r], s, act, g, wcur, gw_acc, s0,
+                                           gh + static_cast<size_t>(tab.row_ptr[r]) * z + s, t < a.T - 1, t > 0,
+                                           tab.row_sfx[r] != 0, d0, seed_t);
                 s0 = s1;
                 s1 = s2;
+                d0 = d1;
+                d1 = d2;
                 if (r > 0 && tab.sync_after[r - 1]) __syncthreads();
             }
             __syncthreads();
@@ -540,21 +627,50 @@ __global__ void adam_kernel(int n, float* w, const double* grad, float* m, float
 
 }  // namespace
 
+// Shared memory: header, weight rows, two core-column buffers per codeword.
 size_t wms_smem_bytes(const CodeTable& tab, int cpb) {
-    return kHdr + 2 * kMaxEdges * sizeof(float) + 2 * static_cast<size_t>(cpb) * tab.n_bp * sizeof(float);
+    return kHdr + 2 * kMaxEdges * sizeof(float) + 2 * static_cast<size_t>(cpb) * tab.core_floats * sizeof(float);
 }
 
-cudaError_t wms_kernel_attributes(size_t smem) {
-    const void* ks[4] = {reinterpret_cast<const void*>(&wms_forward_kernel<false>),
-                         reinterpret_cast<const void*>(&wms_forward_kernel<true>),
-                         reinterpret_cast<const void*>(&wms_backward_kernel),
-                         reinterpret_cast<const void*>(&wms_backward_layered_kernel)};
-    for (const void* k : ks) {
-        cudaError_t e =
-            cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-        if (e != cudaSuccess) return e;
+namespace {
+// kernel k of the degree class: 0 forward flooding, 1 forward layered,
+// 2 adjoint flooding, 3 adjoint layered
+template <int MAXD>
+const void* wms_kernel(int k) {
+    switch (k) {
+        case 0: return reinterpret_cast<const void*>(&wms_forward_kernel<MAXD, false>);
+        case 1: return reinterpret_cast<const void*>(&wms_forward_kernel<MAXD, true>);
+        case 2: return reinterpret_cast<const void*>(&wms_backward_kernel<MAXD>);
+        default: return reinterpret_cast<const void*>(&wms_backward_layered_kernel<MAXD>);
     }
+}
+const void* wms_kernel_for(const CodeTable& tab, int k) {
+    int maxd = 0;
+    for (int r = 0; r < tab.rows; r++) maxd = tab.row_deg[r] > maxd ? tab.row_deg[r] : maxd;
+    return maxd <= 10 ? wms_kernel<10>(k) : wms_kernel<19>(k);
+}
+}  // namespace
+
+cudaError_t wms_kernel_attributes(size_t smem) {
+    for (int k = 0; k < 4; k++)
+        for (const void* f : {wms_kernel<10>(k), wms_kernel<19>(k)}) {
+            cudaError_t e =
+                cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+            if (e != cudaSuccess) return e;
+        }
     return cudaSuccess;
+}
+
+int wms_ctas_per_sm(const CodeTable& tab, int threads, size_t smem) {
+    int n = 1 << 30;
+    for (int k = 0; k < 4; k++) {
+        int c = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, wms_kernel_for(tab, k), threads, smem) !=
+            cudaSuccess)
+            return 0;
+        n = c < n ? c : n;
+    }
+    return n;
 }
 
 cudaError_t launch_wms(bool backward, bool layered, const CodeTable& tab, const float* llr, const uint8_t* cw,
@@ -580,15 +696,9 @@ cudaError_t launch_wms(bool backward, bool layered, const CodeTable& tab, const 
     a.n_groups = (n_cw + cpb - 1) / cpb;
     a.scale = scale;
     grid = grid < a.n_groups ? grid : a.n_groups;
-    if (backward && layered)
-        wms_backward_layered_kernel<<<grid, threads, smem, stream>>>(tab, a);
-    else if (backward)
-        wms_backward_kernel<<<grid, threads, smem, stream>>>(tab, a);
-    else if (layered)
-        wms_forward_kernel<true><<<grid, threads, smem, stream>>>(tab, a);
-    else
-        wms_forward_kernel<false><<<grid, threads, smem, stream>>>(tab, a);
-    return cudaGetLastError();
+    const void* k = wms_kernel_for(tab, (backward ? 2 : 0) + (layered ? 1 : 0));
+    void* params[2] = {const_cast<CodeTable*>(&tab), &a};
+    return cudaLaunchKernel(k, dim3(grid), dim3(threads), params, smem, stream);
 }
 
 cudaError_t launch_adam(int n, float* w, const double* grad, float* m, float* v, int step, float lr,
