@@ -221,9 +221,18 @@ typedef struct nrldpc_batch nrldpc_batch;
 /* Tables of every (bg, z) on `device`, scratch for up to max_jobs jobs. */
 int nrldpc_batch_create(int device, int max_jobs, float alpha, nrldpc_batch** out);
 int nrldpc_batch_destroy(nrldpc_batch* b);
-/* Codewords per CTA for one code (the autotuner's knob); 0 restores the default. */
+/* Launch geometry per code, the autotuner's two knobs (the reference fixes
+ * it: one thread per sub-row, roundup32(Z) x codewords per block,
+ * src/setup_exp.cu:131-166).  Codewords per CTA: 0 restores the largest that
+ * the CTA's 384 threads and shared memory admit.  Sub-rows per thread 1 or 2
+ * (0 = 1): threads per codeword = Z / spt, thread t owning sub-rows t and
+ * t + Z/2 (Z even); changing it clamps codewords per CTA to what fits.  The
+ * batch's CTA has the threads of its widest work item.  Results do not
+ * depend on either knob.  Apply before nrldpc_batch_set_jobs. */
 int nrldpc_batch_set_cw_per_cta(nrldpc_batch* b, int bg, int z, int cw_per_cta);
 int nrldpc_batch_get_cw_per_cta(nrldpc_batch* b, int bg, int z, int* cw_per_cta);
+int nrldpc_batch_set_sub_rows_per_thread(nrldpc_batch* b, int bg, int z, int sub_rows_per_thread);
+int nrldpc_batch_get_sub_rows_per_thread(nrldpc_batch* b, int bg, int z, int* sub_rows_per_thread);
 /* Load a job list (host array): validated, grouped by code into the device
  * work queue (largest work first).  Synchronous. */
 int nrldpc_batch_set_jobs(nrldpc_batch* b, const nrldpc_job* jobs, int n_jobs);

@@ -67,6 +67,8 @@ SIGNATURES = {
     "nrldpc_batch_destroy": (_i, [_vp]),
     "nrldpc_batch_set_cw_per_cta": (_i, [_vp, _i, _i, _i]),
     "nrldpc_batch_get_cw_per_cta": (_i, [_vp, _i, _i, _ip]),
+    "nrldpc_batch_set_sub_rows_per_thread": (_i, [_vp, _i, _i, _i]),
+    "nrldpc_batch_get_sub_rows_per_thread": (_i, [_vp, _i, _i, _ip]),
     "nrldpc_batch_set_jobs": (_i, [_vp, _vp, _i]),
     "nrldpc_batch_gen": (_i, [_vp, _u64, _u64, _vp, _vp, _vp]),
     "nrldpc_batch_derate": (_i, [_vp, _vp, _vp, _vp]),

@@ -50,6 +50,25 @@ def make_jobs(bg, z, k_prime=0, e=0, rv=0, sigma=1.0, qm=1):
     return jobs, int(llr_len.sum()), int(ee.sum()), int(pb.sum())
 
 
+MIXED_ZS = (64, 96, 128, 192, 256, 320, 384)
+
+
+def mixed_workload(n: int = 8192, seed: int = 2024):
+    """The uneven-batch workload: n codewords, BG1 or BG2 uniformly, Z uniform
+    in {64, ..., 384}, up to 39 filler bits, code rate K'/E uniform in
+    [0.25, 0.8] (E at least 2Z + 8), Eb/N0 uniform in 1-3 dB.  Returns
+    (bg, z, k_prime, e, sigma) arrays."""
+    rng = np.random.default_rng(seed)
+    bg = rng.integers(1, 3, n)
+    z = rng.choice(MIXED_ZS, n)
+    kb = np.where(bg == 1, 22, 10)
+    kp = kb * z - rng.integers(0, 40, n)
+    e = np.maximum((kp / rng.uniform(0.25, 0.8, n)).astype(np.int64), 2 * z + 8)
+    eb = rng.uniform(1.0, 3.0, n)
+    sigma = np.sqrt((e / kp) / (2.0 * 10 ** (eb / 10))).astype(np.float32)
+    return bg, z, kp, e, sigma
+
+
 class Batch:
     def __init__(self, max_jobs: int, alpha: float = 0.75, device: int = 0):
         self.lib = _lib.load()
@@ -59,8 +78,9 @@ class Batch:
         self.device = torch.device("cuda", device)
         self.jobs = None
         from .autotune import load_table
-        for (bg, z), cpb in load_table(device).items():  # tuned codewords per CTA, if any
+        for (bg, z), (cpb, spt) in load_table(device).items():  # tuned geometry, if any
             try:
+                self.set_sub_rows_per_thread(bg, z, spt)
                 self.set_cw_per_cta(bg, z, cpb)
             except _lib.NrLdpcError:
                 pass
@@ -82,6 +102,17 @@ class Batch:
     def get_cw_per_cta(self, bg: int, z: int) -> int:
         v = C.c_int()
         _lib.check("nrldpc_batch_get_cw_per_cta", self.lib.nrldpc_batch_get_cw_per_cta(self._h, bg, z, C.byref(v)))
+        return v.value
+
+    def set_sub_rows_per_thread(self, bg: int, z: int, spt: int):
+        """Threads per codeword = Z / spt (spt 1 or 2); apply before set_jobs."""
+        _lib.check("nrldpc_batch_set_sub_rows_per_thread",
+                   self.lib.nrldpc_batch_set_sub_rows_per_thread(self._h, bg, z, spt))
+
+    def get_sub_rows_per_thread(self, bg: int, z: int) -> int:
+        v = C.c_int()
+        _lib.check("nrldpc_batch_get_sub_rows_per_thread",
+                   self.lib.nrldpc_batch_get_sub_rows_per_thread(self._h, bg, z, C.byref(v)))
         return v.value
 
     def set_jobs(self, jobs: np.ndarray):

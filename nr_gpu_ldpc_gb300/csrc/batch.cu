@@ -231,7 +231,7 @@ struct Batch {
     CodeTable h_tables[kNumCodes];
     bool code_ok[kNumCodes];
     int cpb[kNumCodes];
-    int cpb_default[kNumCodes];
+    int spt[kNumCodes];  // sub-rows per thread (threads per codeword = Z / spt)
     CodeTable* d_tables = nullptr;
     PlanDev* d_plans = nullptr;
     // job list
@@ -242,7 +242,7 @@ struct Batch {
     int32_t* d_order = nullptr;
     WorkItem* d_items = nullptr;
     size_t slot_words = 0, smem = 0;
-    int grid = 0;
+    int grid = 0, threads = kMaxThreads;
     uint32_t* d_state = nullptr;
     size_t state_words = 0;
     int* d_scratch = nullptr;
@@ -254,6 +254,18 @@ struct Batch {
 };
 
 int map_cuda(cudaError_t e) { return e == cudaSuccess ? NRLDPC_OK : NRLDPC_ERR_CUDA; }
+
+// Most codewords per CTA of code id with spt sub-rows per thread: Z / spt
+// threads each within kMaxThreads, and their shared memory within the
+// device's opt-in limit.
+int max_cpb(const Batch* b, int id, int spt) {
+    const CodeTable& t = b->h_tables[id];
+    const int tpc = t.z / spt;
+    const size_t room = b->smem_optin - kHeaderBytesBatch - kBatchTableBytes;
+    int c = std::max(1, kMaxThreads / tpc);
+    while (c > 1 && group_smem_bytes(t, c) > room) c--;
+    return std::min(c, 48);
+}
 
 int code_id(int bg, int z) {
     const int zi = z_index(z);
@@ -329,11 +341,10 @@ int nrldpc_batch_create(int device, int max_jobs, float alpha, nrldpc_batch** ou
                     pd.step_col[k] = static_cast<uint8_t>(ep.core_col[k]);
                 }
             }
-            // default: as many codewords as 384 threads and shared memory allow
-            const size_t room = b->smem_optin - kHeaderBytesBatch - kBatchTableBytes;
-            int c = std::max(1, kMaxThreads / z);
-            while (c > 1 && group_smem_bytes(t, c) > room) c--;
-            b->cpb_default[id] = b->cpb[id] = std::min(c, 48);
+            // default: one sub-row per thread, as many codewords as 384
+            // threads and shared memory allow
+            b->spt[id] = 1;
+            b->cpb[id] = max_cpb(b, id, 1);
         }
     if (cudaMalloc(&b->d_tables, sizeof(CodeTable) * kNumCodes) != cudaSuccess ||
         cudaMalloc(&b->d_plans, sizeof(PlanDev) * kNumCodes) != cudaSuccess ||
@@ -366,9 +377,29 @@ int nrldpc_batch_set_cw_per_cta(nrldpc_batch* batch, int bg, int z, int cpb) {
     Batch* b = reinterpret_cast<Batch*>(batch);
     const int id = b ? code_id(bg, z) : -1;
     if (!b || id < 0 || cpb < 0) return NRLDPC_ERR_INVALID_ARG;
-    if (cpb == 0) cpb = b->cpb_default[id];
-    if (cpb > b->cpb_default[id]) return NRLDPC_ERR_BAD_CONFIG;  // threads or shared memory
+    const int most = max_cpb(b, id, b->spt[id]);
+    if (cpb == 0) cpb = most;
+    if (cpb > most) return NRLDPC_ERR_BAD_CONFIG;  // threads or shared memory
     b->cpb[id] = cpb;
+    return NRLDPC_OK;
+}
+
+int nrldpc_batch_set_sub_rows_per_thread(nrldpc_batch* batch, int bg, int z, int spt) {
+    Batch* b = reinterpret_cast<Batch*>(batch);
+    const int id = b ? code_id(bg, z) : -1;
+    if (!b || id < 0 || spt < 0 || spt > 2) return NRLDPC_ERR_INVALID_ARG;
+    if (spt == 0) spt = 1;
+    if (z % spt != 0) return NRLDPC_ERR_BAD_CONFIG;  // sub-rows s and s + Z/2
+    b->spt[id] = spt;
+    b->cpb[id] = std::min(b->cpb[id], max_cpb(b, id, spt));
+    return NRLDPC_OK;
+}
+
+int nrldpc_batch_get_sub_rows_per_thread(nrldpc_batch* batch, int bg, int z, int* spt) {
+    Batch* b = reinterpret_cast<Batch*>(batch);
+    const int id = b ? code_id(bg, z) : -1;
+    if (!b || id < 0 || !spt) return NRLDPC_ERR_INVALID_ARG;
+    *spt = b->spt[id];
     return NRLDPC_OK;
 }
 
@@ -422,15 +453,17 @@ int nrldpc_batch_set_jobs(nrldpc_batch* batch, const nrldpc_job* jobs, int n_job
     });
     std::vector<WorkItem> items;
     size_t slot_words = 0, bufs = 0;
+    int threads = 32;
     for (int i = 0; i < n_jobs;) {
         const int id = b->h_jobs[order[i]].code;
         int k = i;
         while (k < n_jobs && b->h_jobs[order[k]].code == id) k++;
-        const int cpb = b->cpb[id];
+        const int cpb = b->cpb[id], spt = b->spt[id];
         const CodeTable& t = b->h_tables[id];
         for (int s = i; s < k; s += cpb) {
             const int cnt = std::min(cpb, k - s);
-            items.push_back(WorkItem{id, s, cnt, 0});
+            items.push_back(WorkItem{id, s, cnt, spt});
+            threads = std::max(threads, (cnt * (t.z / spt) + 31) / 32 * 32);
             slot_words = std::max(slot_words, static_cast<size_t>(cnt) * 4 * t.rows * t.z);
             bufs = std::max(bufs, group_smem_bytes(t, cnt));
         }
@@ -440,8 +473,9 @@ int nrldpc_batch_set_jobs(nrldpc_batch* batch, const nrldpc_job* jobs, int n_job
     b->n_items = static_cast<int>(items.size());
     b->slot_words = slot_words;
     b->smem = kHeaderBytesBatch + kBatchTableBytes + bufs;
+    b->threads = threads;  // the widest work item's threads
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_decode_kernel_ptr(), kMaxThreads, b->smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_decode_kernel_ptr(), b->threads, b->smem);
     b->grid = std::max(1, std::min(b->n_items, std::max(per_sm, 1) * b->sm_count));
     const size_t need = static_cast<size_t>(b->grid) * std::max<size_t>(slot_words, 1);
     if (need > b->state_words) {
@@ -521,7 +555,7 @@ int nrldpc_batch_decode(nrldpc_batch* batch, const float* d_llr, uint8_t* d_pack
     cudaKernelNodeParams kp{};
     kp.func = const_cast<void*>(batch_decode_kernel_ptr());
     kp.gridDim = dim3(b->grid);
-    kp.blockDim = dim3(kMaxThreads);
+    kp.blockDim = dim3(b->threads);
     kp.sharedMemBytes = static_cast<unsigned int>(b->smem);
     kp.kernelParams = params;
     if (!b->exec) {  // memset of the queue head, then the persistent kernel

@@ -296,16 +296,19 @@ __device__ __forceinline__ int edge_pos(const CodeTable& tab, int e, uint32_t s)
 }
 
 // Hard decisions (and optionally posterior / iteration count) of one codeword
-// slot, written by the slot's Z threads.  L: core-column posteriors in shared
+// slot at the bytes / positions of sub-row s (the slot's threads call it once
+// per sub-row they own; tpc = threads per codeword).  L: core-column posteriors in shared
 // memory; hd: the slot's suffix hard-decision bytes, bit `bit` taken; the
 // suffix posteriors come from the state slot when app_from_state (otherwise
 // the row pass already wrote them).
 __device__ __forceinline__ void write_outputs(const CodeTable& tab, const float* L, const uint8_t* hd,
-                                              int bit, const uint4* st_slot, uint32_t s, uint8_t* packed,
-                                              float* app, int32_t* iters, int it, bool app_from_state) {
+                                              int bit, const uint4* st_slot, uint32_t s, uint32_t tpc,
+                                              uint8_t* packed, float* app, int32_t* iters, int it,
+                                              bool app_from_state) {
     const int n = tab.n_bp, z = tab.z, ncz = tab.n_core * z;
-    if ((z & 31) == 0) {
-        // Warp ballots (the slot is whole warps): thread s decides positions
+    if ((tpc & 31u) == 0) {
+        // Warp ballots (the slot is whole warps of tpc threads, each calling
+        // for sub-row s): thread s decides positions
         // s + k*Z (column k, sub-position s); one ballot over a warp is the
         // 32 bits of positions 32*w .. 32*w + 31, LSB first = 4 packed bytes.
         const uint32_t lane = s & 31u;
@@ -366,38 +369,55 @@ __device__ __forceinline__ void write_outputs(const CodeTable& tab, const float*
 // All base rows of one iteration, ascending.  The state of row r+2 is
 // requested while row r runs (L2 latency spans more than one row); in the
 // first iteration the state is zero and only the suffix posterior is
-// fetched, from the codeword's LLRs in global memory.
+// fetched, from the codeword's LLRs in global memory.  SPT = 2: the thread
+// owns sub-rows s and s + tpc and runs both in each row, the state of the
+// next row's two sub-rows requested while this row's run.
 //   store: write this iteration's state; write_hd: write the suffix hard
 //   decisions.
-template <bool WEIGHTED, bool LAYERED>
-__device__ __forceinline__ void iterate_rows(const CodeTable& tab, uint32_t s, uint32_t s4old, uint32_t dnew,
-                                             const float4* wpad, uint4* st_base,
+template <bool WEIGHTED, bool LAYERED, int SPT>
+__device__ __forceinline__ void iterate_rows(const CodeTable& tab, uint32_t s, uint32_t tpc, uint32_t s4old,
+                                             uint32_t dnew, const float4* wpad, uint4* st_base,
                                              const float* gllr,
                                              uint32_t hd_base, bool act, bool first, bool store, bool write_hd,
                                              float alpha) {
     const int z = tab.z, rows = tab.rows;
     const uint32_t z4 = 4u * static_cast<uint32_t>(z);
-    auto fetch = [&](int r) -> uint4 {
+    auto fetch = [&](int r, uint32_t sj) -> uint4 {
         uint4 v = make_uint4(0u, 0u, 0u, 0u);
         if (!act || r >= rows) return v;
-        if (!first) return __ldcg(st_base + r * z + s);
-        if (tab.row_sfx[r]) v.w = __float_as_uint(__ldcs(gllr + edge_pos(tab, tab.row_ptr[r + 1] - 1, s)));
+        if (!first) return __ldcg(st_base + r * z + sj);
+        if (tab.row_sfx[r]) v.w = __float_as_uint(__ldcs(gllr + edge_pos(tab, tab.row_ptr[r + 1] - 1, sj)));
         return v;
     };
-    uint4 s0 = fetch(0), s1 = fetch(1);
-    for (int r = 0; r < rows; r++) {
-        const uint4 s2 = fetch(r + 2);
-        if (act) {
-            const bool sfx = tab.row_sfx[r] != 0;
-            row_dispatch<WEIGHTED, LAYERED>(tab.row_deg[r], tab, tab.row_ptr[r], sfx, s, s4old, dnew, z4,
-                                            wpad + r * (kWPad / 4), wpad + (kMaxRows + r) * (kWPad / 4),
-                                            s0, store ? st_base + r * z + s : nullptr,
-                                            (write_hd && sfx) ? hd_base + static_cast<uint32_t>(r * z) : 0u,
-                                            alpha);
+    auto run = [&](int r, uint32_t j, uint4 st) {
+        const uint32_t sj = s + j * tpc;
+        const bool sfx = tab.row_sfx[r] != 0;
+        row_dispatch<WEIGHTED, LAYERED>(tab.row_deg[r], tab, tab.row_ptr[r], sfx, sj, s4old + 4u * j * tpc, dnew,
+                                        z4, wpad + r * (kWPad / 4), wpad + (kMaxRows + r) * (kWPad / 4), st,
+                                        store ? st_base + r * z + sj : nullptr,
+                                        (write_hd && sfx) ? hd_base + j * tpc + static_cast<uint32_t>(r * z) : 0u,
+                                        alpha);
+    };
+    if constexpr (SPT == 1) {
+        uint4 s0 = fetch(0, s), s1 = fetch(1, s);
+        for (int r = 0; r < rows; r++) {
+            const uint4 s2 = fetch(r + 2, s);
+            if (act) run(r, 0, s0);
+            s0 = s1;
+            s1 = s2;
+            if (tab.sync_after[r]) __syncthreads();
         }
-        s0 = s1;
-        s1 = s2;
-        if (tab.sync_after[r]) __syncthreads();
+    } else {
+        uint4 a0 = fetch(0, s), a1 = fetch(0, s + tpc);
+        for (int r = 0; r < rows; r++) {
+            const uint4 b0 = fetch(r + 1, s);
+            if (act) run(r, 0, a0);
+            const uint4 b1 = fetch(r + 1, s + tpc);
+            if (act) run(r, 1, a1);
+            a0 = b0;
+            a1 = b1;
+            if (tab.sync_after[r]) __syncthreads();
+        }
     }
 }
 
@@ -536,8 +556,8 @@ struct SlotOut {
 // Lold in place.  Early stop: after iteration t < n_iter - 1, a codeword
 // whose hard decisions satisfy every check stops with iters = t + 1 (the
 // oracle's rule, ldpc_oracle.c decode_one_f32).
-template <bool WEIGHTED, bool LAYERED>
-__device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slot, uint32_t s,
+template <bool WEIGHTED, bool LAYERED, int SPT = 1>
+__device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slot, uint32_t s, uint32_t tpc,
                                           bool slot_done, float* buf0, uint8_t* hd0,
                                           int* s_fail, uint4* st_base, const float* gllr, SlotOut out,
                                           int n_iter, int early_stop, float alpha, const float* wtab, float4* wpad,
@@ -550,8 +570,9 @@ __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slo
     const uint32_t s4old = smem_addr(lold) + 4u * s;
     const uint32_t dnew = LAYERED ? 0u : static_cast<uint32_t>(cpb) * static_cast<uint32_t>(cf) * 4u;
     const uint32_t hd_base = smem_addr(hd) + s;
+    const int nt = static_cast<int>(tpc);  // threads of the slot
     if (!LAYERED && !slot_done)
-        for (int k = static_cast<int>(s); k < cf / 4; k += z)
+        for (int k = static_cast<int>(s); k < cf / 4; k += nt)
             reinterpret_cast<float4*>(lnew)[k] = reinterpret_cast<const float4*>(lold)[k];
     for (int t = 0; t < n_iter; t++) {
         const bool first = t == 0, last = t == n_iter - 1;
@@ -579,8 +600,8 @@ __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slo
         const bool far_check = __syncthreads_or(!slot_done && s_far[slot] >= kFarRow);
         const bool act = !slot_done;
         const bool store = !last || out.app != nullptr;
-        iterate_rows<WEIGHTED, LAYERED>(tab, s, s4old, dnew, wpad, st_base, gllr, hd_base, act, first, store,
-                                        early_stop || last, alpha);
+        iterate_rows<WEIGHTED, LAYERED, SPT>(tab, s, tpc, s4old, dnew, wpad, st_base, gllr, hd_base, act, first,
+                                             store, early_stop || last, alpha);
         if (early_stop && !last) {  // the rows ended with a barrier
             // bit-sliced scratch: flooding in Lold (read again only after the
             // copy-back below), layered in the weight rows (restaged at the
@@ -591,20 +612,27 @@ __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slo
                            LAYERED ? reinterpret_cast<uint32_t*>(wpad) : reinterpret_cast<uint32_t*>(buf0), s_fail,
                            s_far);
             else if (act)
-                check_rows(tab, s, s4old + dnew, hd_base, &s_fail[slot], &s_far[slot]);
+                for (int j = 0; j < SPT; j++)
+                    check_rows(tab, s + j * tpc, s4old + 4u * j * tpc + dnew, hd_base + j * tpc, &s_fail[slot],
+                               &s_far[slot]);
             __syncthreads();
             const bool conv = act && s_fail[slot] == 0;
             if (conv)  // HD of this iteration is a codeword
-                write_outputs(tab, lnew, hd, 1, st_base, s, out.packed, out.app, out.iters, t + 1, true);
+                for (int j = 0; j < SPT; j++)
+                    write_outputs(tab, lnew, hd, 1, st_base, s + j * tpc, tpc, out.packed, out.app, out.iters, t + 1,
+                                  true);
             slot_done = slot_done || conv;
             if (__syncthreads_and(slot_done)) break;
         }
         if (last) {
-            if (!slot_done) write_outputs(tab, lnew, hd, 1, st_base, s, out.packed, out.app, out.iters, n_iter, true);
+            if (!slot_done)
+                for (int j = 0; j < SPT; j++)
+                    write_outputs(tab, lnew, hd, 1, st_base, s + j * tpc, tpc, out.packed, out.app, out.iters, n_iter,
+                                  true);
             break;
         }
         if (!LAYERED && !slot_done)  // the posterior just accumulated is the next iteration's input
-            for (int k = static_cast<int>(s); k < cf / 4; k += z)
+            for (int k = static_cast<int>(s); k < cf / 4; k += nt)
                 reinterpret_cast<float4*>(lold)[k] = reinterpret_cast<const float4*>(lnew)[k];
     }
     __syncthreads();  // buffers are rewritten by the next group's copy
@@ -703,8 +731,9 @@ __global__ void __launch_bounds__(kMaxThreads, MINB)
         const size_t cw = static_cast<size_t>(cw0 + (slot_done ? 0 : slot));
         SlotOut out{a.packed + cw * tab.packed_bytes, a.app ? a.app + cw * n : nullptr,
                     a.iters ? a.iters + cw : nullptr};
-        run_group<WEIGHTED, LAYERED>(tab, cpb, slot, s, slot_done, buf0, hd0, s_fail, st_base, a.llr + cw * n, out,
-                                     a.n_iter, a.early_stop, a.alpha, wtab, wpad, a.n_w_iters);
+        run_group<WEIGHTED, LAYERED>(tab, cpb, slot, s, static_cast<uint32_t>(z), slot_done, buf0, hd0, s_fail,
+                                     st_base, a.llr + cw * n, out, a.n_iter, a.early_stop, a.alpha, wtab, wpad,
+                                     a.n_w_iters);
     }
 }
 
@@ -742,9 +771,10 @@ __global__ void __launch_bounds__(kMaxThreads, 2)
         __syncthreads();
         const CodeTable& tab = *stab;
         const int z = tab.z, cf = tab.core_floats, cpb = item.count;
+        const int tpc = z / item.spt;  // threads per codeword: each owns spt sub-rows
         uint8_t* hd0 = reinterpret_cast<uint8_t*>(buf0 + 2 * static_cast<size_t>(cpb) * cf);
-        const int slot = tid / z;
-        const uint32_t s = static_cast<uint32_t>(tid - slot * z);
+        const int slot = tid / tpc;
+        const uint32_t s = static_cast<uint32_t>(tid - slot * tpc);
         const bool valid_thread = slot < cpb;
         if (tid == 0) {
             fence_proxy_async();
@@ -768,8 +798,14 @@ __global__ void __launch_bounds__(kMaxThreads, 2)
         SlotOut out{a.packed + job.out_offset, nullptr, a.iters ? a.iters + jidx : nullptr};
         uint4* st_base = reinterpret_cast<uint4*>(a.state + static_cast<size_t>(blockIdx.x) * a.slot_words) +
                          static_cast<size_t>(valid_thread ? slot : 0) * tab.rows * z;
-        run_group<false, false>(tab, cpb, slot, s, !valid_thread, buf0, hd0, s_fail, st_base,
-                         a.llr + job.llr_offset, out, a.n_iter, a.early_stop, a.alpha, nullptr, nullptr, 1);
+        if (item.spt == 2)
+            run_group<false, false, 2>(tab, cpb, slot, s, static_cast<uint32_t>(tpc), !valid_thread, buf0, hd0,
+                                       s_fail, st_base, a.llr + job.llr_offset, out, a.n_iter, a.early_stop, a.alpha,
+                                       nullptr, nullptr, 1);
+        else
+            run_group<false, false, 1>(tab, cpb, slot, s, static_cast<uint32_t>(tpc), !valid_thread, buf0, hd0,
+                                       s_fail, st_base, a.llr + job.llr_offset, out, a.n_iter, a.early_stop, a.alpha,
+                                       nullptr, nullptr, 1);
     }
 }
 
@@ -798,8 +834,9 @@ const void* select_kernel(bool weighted, int minb, bool layered, bool from_host 
     return minb >= 2 ? kernel_ptr<false, 2, false>() : kernel_ptr<false, 1, false>();
 }
 
-cudaError_t launch_batch_decode(const BatchDecodeArgs& args, int grid, size_t smem, cudaStream_t stream) {
-    batch_decode_kernel<<<grid, kMaxThreads, smem, stream>>>(args);
+cudaError_t launch_batch_decode(const BatchDecodeArgs& args, int grid, int threads, size_t smem,
+                                cudaStream_t stream) {
+    batch_decode_kernel<<<grid, threads, smem, stream>>>(args);
     return cudaGetLastError();
 }
 

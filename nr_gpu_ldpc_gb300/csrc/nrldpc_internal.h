@@ -91,7 +91,7 @@ struct WorkItem {
     int32_t code;   // index into the table array
     int32_t start;
     int32_t count;
-    int32_t pad;
+    int32_t spt;    // sub-rows per thread: Z / spt threads per codeword (1 or 2)
 };
 constexpr size_t kHeaderBytesBatch = 1024;  // mbarrier, item id, per-slot flags
 constexpr size_t kBatchTableCopy = (offsetof(CodeTable, eaddr) + 15) / 16 * 16;
@@ -118,7 +118,8 @@ inline size_t group_smem_bytes(const CodeTable& t, int cpb) {
     const size_t hd = (static_cast<size_t>(cpb) * t.rows * t.z + 15) / 16 * 16;
     return 2 * static_cast<size_t>(cpb) * t.core_floats * sizeof(float) + hd;
 }
-cudaError_t launch_batch_decode(const BatchDecodeArgs& args, int grid, size_t smem, cudaStream_t stream);
+cudaError_t launch_batch_decode(const BatchDecodeArgs& args, int grid, int threads, size_t smem,
+                                cudaStream_t stream);
 const void* batch_decode_kernel_ptr();
 
 // Host-side launchers (decode.cu / channel.cu).

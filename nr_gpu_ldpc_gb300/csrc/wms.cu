@@ -43,6 +43,31 @@ __device__ __forceinline__ float max_nan(float a, float b) {
 
 __device__ __forceinline__ int cw_bit(const uint8_t* cw, int c) { return (cw[c >> 3] >> (c & 7)) & 1; }
 
+// Per-thread asynchronous copies global -> shared (each thread waits only
+// for its own groups; the sources are in-bounds device memory, so every
+// copy completes).
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// The BG2 flooding adjoint stages each row's state, per-row dloss/dQ and
+// suffix seed through a per-thread ring of kRing rows in shared memory
+// (kRing - 1 rows requested ahead: the rows come from DRAM, where two rows
+// of look-ahead in registers left the kernel waiting on loads).
+constexpr int kRing = 4;
+constexpr size_t kRingBytes = static_cast<size_t>(kRing) * kMaxThreads * (16 + 16 + 4);
+
 // Stored state of one lifted row after iteration t (16 B): min1, min2,
 // info = i1 | i2 << 5 | Q sign bits << 10 (i2 = 31: no second argmin), and
 // the posterior of the row's suffix column at this sub-row after the
@@ -74,11 +99,28 @@ __device__ __forceinline__ float loss_term(float L, bool bit1, float scale, floa
 }
 
 // ---- forward ------------------------------------------------------------------------
+// Forward weights of the iteration in shared memory, one padded row of kWPad
+// floats per base row (previous iteration's rows, then the current ones), so
+// a row's weights come in as 128-bit loads: [2][kMaxRows][kWPad].
+constexpr int kWPad = 20;
+constexpr int kFwdWeightFloats = 2 * kMaxRows * kWPad;
+
+// Weight i of a padded row held as float4s (i is constant after unrolling).
+__device__ __forceinline__ float wsel(const float4* w, int i) {
+    const float4 v = w[i >> 2];
+    const int c = i & 3;
+    return c == 0 ? v.x : c == 1 ? v.y : c == 2 ? v.z : v.w;
+}
+
 // sfx: the row's last edge is a suffix column, its posterior is st.w (read)
 // and the stored state's w (written); its loss term and seed are taken here.
+// Signs: R_old_i's is bit i of the previous Q signs XOR their parity; Q_i's
+// is the sign bit of Q_i + 0 ((Q < 0): -0 gives +0, a NaN result is the
+// canonical positive NaN), collected by a funnel shift (edge i at bit
+// D-1-i) and bit-reversed into the stored order (edge i at bit i).
 template <int D, bool LAYERED>
 __device__ __forceinline__ void fwd_row(const CodeTable& tab, int e0, uint32_t s, const float* lold,
-                                        float* lnew, const float* w_prev, const float* w_cur,
+                                        float* lnew, const float4* w_prev, const float4* w_cur,
                                         uint4 st, uint4* st_out, bool sfx, bool ybit, float* seed_t,
                                         float scale, float* loss) {
     constexpr int LAST = D - 1;
@@ -93,19 +135,18 @@ __device__ __forceinline__ void fwd_row(const CodeTable& tab, int e0, uint32_t s
     const float om1 = __uint_as_float(st.x), om2 = __uint_as_float(st.y);
     const uint32_t oq = st.z >> 10;
     const int oidx = static_cast<int>(st.z & 31u);
-    const uint32_t opar = static_cast<uint32_t>(__popc(oq) & 1);
+    const uint32_t orsign = oq ^ (0u - (static_cast<uint32_t>(__popc(oq)) & 1u));  // R_old_i's sign at bit i
     float m1 = 1000.0f, m2 = 1000.0f;
     int i1 = 0, i2 = 31;
-    uint32_t qmask = 0;
+    uint32_t qrev = 0;
 #pragma unroll
     for (int i = 0; i < D; i++) {
-        const float mag = __fmul_rn(w_prev[e0 + i], i == oidx ? om2 : om1);
-        const uint32_t sb = (opar ^ (oq >> i)) & 1u;
-        rold[i] = __uint_as_float(__float_as_uint(mag) ^ (sb << 31));
+        const float mag = __fmul_rn(wsel(w_prev, i), i == oidx ? om2 : om1);
+        rold[i] = __uint_as_float(__float_as_uint(mag) ^ ((orsign << (31 - i)) & 0x80000000u));
         const float q = __fsub_rn(lv[i], rold[i]);
         if (LAYERED) rold[i] = q;  // the layered update needs Q, not R_old
         const float qa = fabsf(q);
-        if (q < 0.0f) qmask |= 1u << i;
+        qrev = __funnelshift_l(__float_as_uint(__fadd_rn(q, 0.0f)), qrev, 1);
         const bool p1 = qa < m1, p2 = qa < m2;
         i2 = p1 ? i1 : (p2 ? i : i2);
         i1 = p1 ? i : i1;
@@ -113,16 +154,16 @@ __device__ __forceinline__ void fwd_row(const CodeTable& tab, int e0, uint32_t s
         m1 = fminf(m1, qa);
         m2 = fminf(m2, mx);
     }
-    const uint32_t par = static_cast<uint32_t>(__popc(qmask) & 1);
+    const uint32_t qmask = __brev(qrev) >> (32 - D);  // Q_i's sign at bit i
+    const uint32_t rsign = qmask ^ (0u - (static_cast<uint32_t>(__popc(qmask)) & 1u));  // R_new_i's
     float nv[D];
 #pragma unroll
     for (int i = 0; i < D; i++) nv[i] = (LAYERED || (i == LAST && sfx)) ? lv[i] : lnew[addr[i]];
     float sfx_new = 0.0f;
 #pragma unroll
     for (int i = 0; i < D; i++) {
-        const float mag = __fmul_rn(w_cur[e0 + i], i == i1 ? m2 : m1);
-        const uint32_t sb = (par ^ (qmask >> i)) & 1u;
-        const float rn = __uint_as_float(__float_as_uint(mag) ^ (sb << 31));
+        const float mag = __fmul_rn(wsel(w_cur, i), i == i1 ? m2 : m1);
+        const float rn = __uint_as_float(__float_as_uint(mag) ^ ((rsign << (31 - i)) & 0x80000000u));
         // layered: A = Q + R_new; flooding: Lnew += R_new - R_old
         const float v = LAYERED ? __fadd_rn(rold[i], rn) : __fadd_rn(nv[i], __fsub_rn(rn, rold[i]));
         if (i == LAST && sfx)
@@ -146,8 +187,8 @@ __device__ __forceinline__ void fwd_row(const CodeTable& tab, int e0, uint32_t s
 
 template <int MAXD, bool LAYERED>
 __device__ __forceinline__ void fwd_dispatch(int deg, const CodeTable& tab, int e0, uint32_t s,
-                                             const float* lold, float* lnew, const float* wp,
-                                             const float* wc, uint4 st, uint4* st_out, bool sfx, bool ybit,
+                                             const float* lold, float* lnew, const float4* wp,
+                                             const float4* wc, uint4 st, uint4* st_out, bool sfx, bool ybit,
                                              float* seed_t, float scale, float* loss) {
 #define NRLDPC_FWD_CASE(D)                                                                         \
     case D:                                                                                        \
@@ -185,8 +226,9 @@ __global__ void __launch_bounds__(kMaxThreads, kWmsMinBlocks)
     extern __shared__ __align__(128) unsigned char smem[];
     int* s_group = reinterpret_cast<int*>(smem);
     float* s_red = reinterpret_cast<float*>(smem + 64);  // warp partial losses
-    float* wbuf = reinterpret_cast<float*>(smem + kHdr);  // [2][E] previous / current weights
-    float* bufs = wbuf + 2 * kMaxEdges;
+    float* wbuf = reinterpret_cast<float*>(smem + kHdr);  // [2][kMaxRows][kWPad] previous / current
+    const float4* wrow = reinterpret_cast<const float4*>(wbuf);
+    float* bufs = wbuf + kFwdWeightFloats;
     const int z = tab.z, n = tab.n_bp, cpb = a.cpb, rows = tab.rows, E = tab.n_edges;
     const int cf = tab.core_floats, ncz = tab.n_core * z;
     const int tid = threadIdx.x, slot = tid / z;
@@ -226,9 +268,14 @@ __global__ void __launch_bounds__(kMaxThreads, kWmsMinBlocks)
         }
         float loss_part = 0.0f;
         for (int t = 0; t < a.T; t++) {
-            for (int e = tid; e < E; e += blockDim.x) {
-                wbuf[e] = t == 0 ? 0.0f : a.weights[(t - 1) * E + e];
-                wbuf[kMaxEdges + e] = a.weights[t * E + e];
+            for (int k = tid; k < kFwdWeightFloats; k += blockDim.x) {  // padded rows, zero previous at t = 0
+                const int half = k >= kMaxRows * kWPad ? 1 : 0;
+                const int rem = k - half * kMaxRows * kWPad;
+                const int r = rem / kWPad, j = rem - r * kWPad;
+                float v = 0.0f;
+                if (r < rows && j < tab.row_deg[r] && (half || t > 0))
+                    v = a.weights[(t - 1 + half) * E + tab.row_ptr[r] + j];
+                wbuf[k] = v;
             }
             __syncthreads();
             if (act && !LAYERED)
@@ -254,8 +301,9 @@ __global__ void __launch_bounds__(kMaxThreads, kWmsMinBlocks)
             for (int r = 0; r < rows; r++) {
                 const uint4 p2 = fetch(r + 2);
                 if (act)
-                    fwd_dispatch<MAXD, LAYERED>(tab.row_deg[r], tab, tab.row_ptr[r], s, lold, lnew, wbuf,
-                                                wbuf + kMaxEdges, p0, st_cur + r * z + s, tab.row_sfx[r] != 0,
+                    fwd_dispatch<MAXD, LAYERED>(tab.row_deg[r], tab, tab.row_ptr[r], s, lold, lnew,
+                                                wrow + r * (kWPad / 4), wrow + (kMaxRows + r) * (kWPad / 4), p0,
+                                                st_cur + r * z + s, tab.row_sfx[r] != 0,
                                                 (ysfx >> r) & 1u, seed_t, a.scale, &loss_part);
                 p0 = p1;
                 p1 = p2;
@@ -410,6 +458,10 @@ __global__ void __launch_bounds__(kMaxThreads, kWmsMinBlocks)
     const int tid = threadIdx.x, slot = tid / z;
     const uint32_t s = static_cast<uint32_t>(tid - slot * z);
     const bool valid = slot < cpb;
+    // row ring (BG2 kernels): [kRing][blockDim] states, dloss/dQ, seeds
+    uint4* ring_st = reinterpret_cast<uint4*>(bufs + 2 * static_cast<size_t>(cpb) * cf);
+    uint4* ring_gq = ring_st + kRing * blockDim.x;
+    float* ring_sd = reinterpret_cast<float*>(ring_gq + kRing * blockDim.x);
     uint4* gq = a.gq + (static_cast<size_t>(blockIdx.x) * cpb + (valid ? slot : 0)) * rows * z;
     for (;;) {
         if (tid == 0) *s_group = atomicAdd(a.work_counter, 1);
@@ -439,34 +491,61 @@ __global__ void __launch_bounds__(kMaxThreads, kWmsMinBlocks)
             __syncthreads();
             const uint4* st = a.states + (static_cast<size_t>(t) * a.n_cw + (act ? cw : 0)) * rows * z;
             const float* seed_t = a.gseed + (static_cast<size_t>(t) * a.n_cw + (act ? cw : 0)) * n;
-            // state, per-row dloss/dQ and the suffix edge's loss seed of row
-            // r+2 requested while row r runs
-            auto fetch = [&](int r, uint4& sv, uint4& gv, float& sd) {
-                sv = make_uint4(0u, 0u, 31u << 5, 0u);
-                gv = make_uint4(0u, 0u, 31u, 31u);
-                sd = 0.0f;
-                if (act && r < rows) {
-                    sv = __ldcg(st + r * z + s);
-                    gv = __ldcg(gq + r * z + s);
-                    if (tab.row_sfx[r]) sd = __ldcs(seed_t + edge_at(tab.edge[tab.row_ptr[r + 1] - 1], s, z));
+            if constexpr (MAXD <= 10) {
+                // rows r .. r + kRing - 2 in flight in the shared-memory ring
+                const int nt = blockDim.x;
+                auto issue = [&](int r) {
+                    if (act && r < rows) {
+                        const int k = (r % kRing) * nt + tid;
+                        cp_async16(&ring_st[k], st + r * z + s);
+                        cp_async16(&ring_gq[k], gq + r * z + s);
+                        if (tab.row_sfx[r])
+                            cp_async4(&ring_sd[k], seed_t + edge_at(tab.edge[tab.row_ptr[r + 1] - 1], s, z));
+                    }
+                    cp_async_commit();
+                };
+                for (int r = 0; r < kRing - 1; r++) issue(r);
+                for (int r = 0; r < rows; r++) {
+                    issue(r + kRing - 1);
+                    cp_async_wait<kRing - 1>();  // this thread's copies of row r have landed
+                    const int k = (r % kRing) * nt + tid;
+                    const uint4 sv = act ? ring_st[k] : make_uint4(0u, 0u, 31u << 5, 0u);
+                    const uint4 gv = act ? ring_gq[k] : make_uint4(0u, 0u, 31u, 31u);
+                    const float sd = (act && tab.row_sfx[r]) ? ring_sd[k] : 0.0f;
+                    bwd_dispatch<MAXD>(tab.row_deg[r], tab, tab.row_ptr[r], s, act, gl, gln, wcur, gw_acc, sv, gv,
+                                       gq + r * z + s, t > 0, tab.row_sfx[r] != 0, sd);
                 }
-            };
-            uint4 s0, g0, s1, g1;
-            float d0, d1;
-            fetch(0, s0, g0, d0);
-            fetch(1, s1, g1, d1);
-            for (int r = 0; r < rows; r++) {
-                uint4 s2, g2;
-                float d2;
-                fetch(r + 2, s2, g2, d2);
-                bwd_dispatch<MAXD>(tab.row_deg[r], tab, tab.row_ptr[r], s, act, gl, gln, wcur, gw_acc, s0, g0,
-                                   gq + r * z + s, t > 0, tab.row_sfx[r] != 0, d0);
-                s0 = s1;
-                g0 = g1;
-                d0 = d1;
-                s1 = s2;
-                g1 = g2;
-                d1 = d2;
+                cp_async_wait<0>();
+            } else {
+                // state, per-row dloss/dQ and the suffix edge's loss seed of
+                // row r+2 requested while row r runs
+                auto fetch = [&](int r, uint4& sv, uint4& gv, float& sd) {
+                    sv = make_uint4(0u, 0u, 31u << 5, 0u);
+                    gv = make_uint4(0u, 0u, 31u, 31u);
+                    sd = 0.0f;
+                    if (act && r < rows) {
+                        sv = __ldcg(st + r * z + s);
+                        gv = __ldcg(gq + r * z + s);
+                        if (tab.row_sfx[r]) sd = __ldcs(seed_t + edge_at(tab.edge[tab.row_ptr[r + 1] - 1], s, z));
+                    }
+                };
+                uint4 s0, g0, s1, g1;
+                float d0, d1;
+                fetch(0, s0, g0, d0);
+                fetch(1, s1, g1, d1);
+                for (int r = 0; r < rows; r++) {
+                    uint4 s2, g2;
+                    float d2;
+                    fetch(r + 2, s2, g2, d2);
+                    bwd_dispatch<MAXD>(tab.row_deg[r], tab, tab.row_ptr[r], s, act, gl, gln, wcur, gw_acc, s0, g0,
+                                       gq + r * z + s, t > 0, tab.row_sfx[r] != 0, d0);
+                    s0 = s1;
+                    g0 = g1;
+                    d0 = d1;
+                    s1 = s2;
+                    g1 = g2;
+                    d1 = d2;
+                }
             }
             __syncthreads();
             for (int e = tid; e < E; e += blockDim.x)
@@ -627,9 +706,20 @@ __global__ void adam_kernel(int n, float* w, const double* grad, float* m, float
 
 }  // namespace
 
-// Shared memory: header, weight rows, two core-column buffers per codeword.
+namespace {
+int max_row_degree(const CodeTable& tab) {
+    int maxd = 0;
+    for (int r = 0; r < tab.rows; r++) maxd = tab.row_deg[r] > maxd ? tab.row_deg[r] : maxd;
+    return maxd;
+}
+}  // namespace
+
+// Shared memory: header, weight rows (the forward's padded layout, larger than
+// the adjoints' two [E] arrays), two core-column buffers per codeword, and
+// for codes of row degree <= 10 the flooding adjoint's row ring.
 size_t wms_smem_bytes(const CodeTable& tab, int cpb) {
-    return kHdr + 2 * kMaxEdges * sizeof(float) + 2 * static_cast<size_t>(cpb) * tab.core_floats * sizeof(float);
+    return kHdr + kFwdWeightFloats * sizeof(float) + 2 * static_cast<size_t>(cpb) * tab.core_floats * sizeof(float) +
+           (max_row_degree(tab) <= 10 ? kRingBytes : 0);
 }
 
 namespace {
@@ -645,9 +735,7 @@ const void* wms_kernel(int k) {
     }
 }
 const void* wms_kernel_for(const CodeTable& tab, int k) {
-    int maxd = 0;
-    for (int r = 0; r < tab.rows; r++) maxd = tab.row_deg[r] > maxd ? tab.row_deg[r] : maxd;
-    return maxd <= 10 ? wms_kernel<10>(k) : wms_kernel<19>(k);
+    return max_row_degree(tab) <= 10 ? wms_kernel<10>(k) : wms_kernel<19>(k);
 }
 }  // namespace
 

@@ -40,7 +40,8 @@ class Decoder:
         lib = _lib.load()
         if cw_per_cta == 0 and base is None:
             from .autotune import load_table
-            cw_per_cta = load_table(device).get((bg, z), 0)
+            cpb, spt = load_table(device).get((bg, z), (0, 1))
+            cw_per_cta = cpb if spt == 1 else 0  # this decoder runs one sub-row per thread
         cfg = _lib.ConfigC(bg=bg if base is None else 0, z=z, max_batch=max_batch, alpha=alpha,
                            device=device, cw_per_cta=cw_per_cta)
         h = C.c_void_p()

@@ -123,6 +123,96 @@ def test_codewords_per_cta_does_not_change_results(gpu):
     assert torch.equal(outs[0], outs[1]) and torch.equal(outs[0], outs[2])
 
 
+@pytest.mark.parametrize("bg,z", [(1, 256), (2, 320), (2, 96), (1, 64)])
+def test_sub_rows_per_thread_do_not_change_results(gpu, bg, z):
+    """Threads per codeword Z (one sub-row each) or Z/2 (two each), at
+    several codewords per CTA, early stop off and on: the same bits and
+    iteration counts, on warp-aligned (Z/2 a multiple of 32) and unaligned
+    (Z/2 = 48) slots."""
+    jobs, n_llr, _, n_out = make_jobs(np.full(150, bg), z)
+    b = Batch(max_jobs=150)
+    llr = torch.randn(n_llr, device=gpu, generator=torch.Generator(device=gpu).manual_seed(z)) * 2.5 + 1.2
+    ref = None
+    for spt in (1, 2):
+        b.set_sub_rows_per_thread(bg, z, spt)
+        b.set_cw_per_cta(bg, z, 0)
+        top = b.get_cw_per_cta(bg, z)
+        for cpb in sorted({1, top}):
+            b.set_cw_per_cta(bg, z, cpb)
+            assert b.get_sub_rows_per_thread(bg, z) == spt and b.get_cw_per_cta(bg, z) == cpb
+            b.set_jobs(jobs)
+            got = []
+            for early in (False, True):
+                p = torch.zeros(n_out, dtype=torch.uint8, device=gpu)
+                it = torch.zeros(len(jobs), dtype=torch.int32, device=gpu)
+                b.decode(llr, p, 8, early_stop=early, iters=it)
+                got += [p, it]
+            torch.cuda.synchronize()
+            if ref is None:
+                ref = got
+            for a, c in zip(ref, got):
+                assert torch.equal(a, c), (spt, cpb)
+    b.close()
+
+
+def test_sub_rows_per_thread_in_a_mixed_batch(gpu):
+    """Two sub-rows per thread for some codes of a mixed list (the CTA then
+    has the threads of its widest work item): every job equals its code's
+    own handle."""
+    jobs, n_llr, _, n_out = make_jobs(np.array([1, 2, 1, 2, 1, 2] * 4), np.array([256, 128, 320, 96, 384, 256] * 4))
+    b = Batch(max_jobs=64)
+    for bg, z in ((1, 256), (2, 96), (1, 320)):
+        b.set_sub_rows_per_thread(bg, z, 2)
+    with pytest.raises(_lib.NrLdpcError):
+        b.set_sub_rows_per_thread(1, 13, 2)  # odd Z has no half
+    b.set_jobs(jobs)
+    llr = torch.randn(n_llr, device=gpu, generator=torch.Generator(device=gpu).manual_seed(8)) * 3 + 1
+    packed = torch.zeros(n_out, dtype=torch.uint8, device=gpu)
+    b.decode(llr, packed, 6, early_stop=True)
+    torch.cuda.synchronize()
+    for (bg, z) in {(int(j["bg"]), int(j["z"])) for j in jobs}:
+        sel = [i for i, j in enumerate(jobs) if j["bg"] == bg and j["z"] == z]
+        dec = Decoder(bg=bg, z=z, max_batch=len(sel))
+        x = torch.stack([llr[jobs[i]["llr_offset"]:jobs[i]["llr_offset"] + dec.n_bp] for i in sel])
+        want = dec.decode(x.contiguous(), 6, early_stop=True)
+        torch.cuda.synchronize()
+        for k, i in enumerate(sel):
+            o = int(jobs[i]["out_offset"])
+            assert torch.equal(packed[o:o + dec.packed_bytes], want[k]), (bg, z)
+    b.close()
+
+
+def test_autotuner_picks_an_admissible_point(gpu):
+    """Each code alone: the tuner times every admissible (sub-rows per
+    thread, codewords per CTA) and returns the fastest of them."""
+    from nr_gpu_ldpc_gb300.autotune import tune
+    res = tune(zs=(96,), bgs=(2,), reps=1, waves=1, verbose=False)
+    (e,) = res["entries"]
+    tried = {(t["sub_rows_per_thread"], t["cw_per_cta"]) for t in e["tried"]}
+    assert {1, 2} <= {spt for spt, _ in tried}
+    assert (e["sub_rows_per_thread"], e["cw_per_cta"]) in tried
+    assert all(cpb * (96 // spt) <= 384 for spt, cpb in tried)
+    assert e["us_per_cw"] == min(t["us_per_cw"] for t in e["tried"])
+
+
+def test_workload_tuner_keeps_a_tried_point_per_code(gpu):
+    """On a job list: every code present gets a point it was timed at, and
+    the tuned batch is no slower than the default one by more than timing
+    noise."""
+    from nr_gpu_ldpc_gb300.autotune import tune_workload
+    bg = np.array([1, 2] * 60)
+    z = np.array([64, 128, 256, 96] * 30)
+    kp = np.where(bg == 1, 22, 10) * z
+    e = (kp * 2.5).astype(np.int64)
+    sigma = np.full(len(bg), 0.8, np.float32)
+    res = tune_workload(bg, z, kp, e, sigma, n_iter=4, reps=1, verbose=False)
+    assert {(x["bg"], x["z"]) for x in res["entries"]} == {(int(a), int(c)) for a, c in zip(bg, z)}
+    for x in res["entries"]:
+        assert (x["sub_rows_per_thread"], x["cw_per_cta"]) in {(t["sub_rows_per_thread"], t["cw_per_cta"])
+                                                              for t in x["tried"]} | {(1, 0)}
+    assert res["batch_ms_tuned"] <= res["batch_ms_default"]
+
+
 def test_uneven_8192_codeword_mix(gpu):
     """The mixed workload at full size: 8192 codewords, BG1/BG2, Z from
     {64..384}, rate matching with filler, Eb/N0 1-3 dB, early stop, 10
