@@ -118,6 +118,14 @@ typedef struct {
     uint8_t* hd;
 } ws_f32;
 
+/* dt = R_new - R_old computed as the fused fmaf(+-a, min, -R_old) -- one
+ * rounding -- instead of two roundings; what a compiler that contracts
+ * ldpc_kernels.cu:308-310 (dt = R_temp - RCache, R_temp ending in a product)
+ * into a fused multiply-add would compute.  Off by default (the source's
+ * semantics, each statement rounded). */
+static int g_fma_dt = 0;
+void orc_set_fma_dt(int on) { g_fma_dt = on != 0; }
+
 static void decode_one_f32(const orc_code* c, const float* llr, int n_iter, float alpha,
                            const float* w, int n_w_iters, int early, ws_f32* ws,
                            uint8_t* packed, float* app, int32_t* iters) {
@@ -157,11 +165,13 @@ static void decode_one_f32(const orc_code* c, const float* llr, int n_iter, floa
                     const float a = w ? w[(t < n_w_iters ? t : n_w_iters - 1) * c->n_edges + e] : alpha;
                     float r_new = a * sign;
                     r_new = r_new * sq;
-                    r_new = r_new * (i != idx_min ? rmin1 : rmin2);
+                    const float m = i != idx_min ? rmin1 : rmin2;
+                    const float sa = r_new;  /* +-a, exact */
+                    r_new = r_new * m;
                     if (t == 0) {
                         dt[e * z + s] = r_new;
                     } else {
-                        const float d = r_new - R[e * z + s];
+                        const float d = g_fma_dt ? fmaf(sa, m, -R[e * z + s]) : r_new - R[e * z + s];
                         dt[e * z + s] = d;
                     }
                     R[e * z + s] = r_new;

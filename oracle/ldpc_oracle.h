@@ -46,6 +46,10 @@ int orc_code_edges(const orc_code* c);
  *   iters   [n_cw] or NULL         iterations after which HD was taken
  * early_stop != 0: stop after iteration t when the syndrome of HD_t is zero.
  * n_threads > 1 decodes codewords on that many POSIX threads. */
+/* Process-wide switch of orc_minsum_f32: compute dt = R_new - R_old as one
+ * fused multiply-add (what a contracting compiler makes of the reference's
+ * dt line) instead of two roundings.  Off by default. */
+void orc_set_fma_dt(int on);
 int orc_minsum_f32(const orc_code* c, const float* llr, int n_cw, int n_iter, float alpha,
                    int early_stop, uint8_t* packed, float* app, int32_t* iters, int n_threads);
 

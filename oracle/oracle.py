@@ -24,12 +24,35 @@ _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
 _lib = None
 
 
+REF_GPU_CUBIN = os.path.join(REF_DIR, "ref_kernels_bg1.cubin")
+REF_GPU_CONST = os.path.join(REF_DIR, "ref_const_bg1.bin")
+REF_GPU_LIB = os.path.join(HERE, "_build", "libref_gpu.so")
+
+
 def build(reference_root: str | None = None, quiet: bool = True) -> None:
-    """Run oracle/Makefile (the oracle, plus oracle/_ref if the reference exists)."""
+    """Run oracle/Makefile (the oracle and the GPU driver of the reference's
+    kernels, plus oracle/_ref if the reference exists), then write the
+    constant-memory image of the reference's own setup for BG1 Z=384 next to
+    its GPU kernels (oracle/_ref/ref_const_bg1.bin)."""
     cmd = ["make", "-C", HERE]
     if reference_root:
         cmd.append(f"REF={reference_root}")
     subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL if quiet else None)
+    if RefEmu.available("bg1") and os.path.exists(REF_GPU_CUBIN):
+        # the table of the reference's own configuration: BG1, lifting set 1, Z = 384
+        base = _bg1_ils1_base()
+        img = RefEmu(base, 384).constant_image()
+        with open(REF_GPU_CONST, "wb") as f:
+            f.write(img)
+
+
+def _bg1_ils1_base() -> np.ndarray:
+    import sys
+    root = os.path.dirname(HERE)
+    if root not in sys.path:
+        sys.path.insert(0, root)
+    from nr_gpu_ldpc_gb300 import codes
+    return codes.base_matrix(1, codes.set_index(384))
 
 
 def lib():
@@ -43,6 +66,7 @@ def lib():
         L.orc_code_new.argtypes = [_i32p, C.c_int, C.c_int, C.c_int]
         L.orc_code_free.argtypes = [C.c_void_p]
         L.orc_code_edges.argtypes = [C.c_void_p]
+        L.orc_set_fma_dt.argtypes = [C.c_int]
         L.orc_minsum_f32.argtypes = [C.c_void_p, _f32p, C.c_int, C.c_int, C.c_float, C.c_int,
                                      _u8p, C.c_void_p, C.c_void_p, C.c_int]
         L.orc_minsum_f64.argtypes = [C.c_void_p, _f64p, C.c_int, C.c_int, C.c_double, C.c_int,
@@ -272,6 +296,7 @@ class RefEmu:
         self.L.ref_setup_ldpc.argtypes = [C.c_int, C.c_float, C.c_int, _i32p]
         self.L.ref_transmit_llr.argtypes = [C.c_int, C.c_float, C.c_int, C.c_float, C.c_uint,
                                             _f32p, _i32p]
+        self.L.ref_constant_image.argtypes = [C.c_void_p, C.c_int]
         h = np.ascontiguousarray(base, np.int32).copy()
         h[h >= 0] %= int(z)
         self.rows, self.cols = h.shape
@@ -303,6 +328,15 @@ class RefEmu:
                 app[s:e] = ap
         return packed, app
 
+    def constant_image(self) -> bytes:
+        """The constant memory the reference's setup writes for this code
+        (one codeword per block column), as the bytes of its kernels' arrays."""
+        buf = (C.c_ubyte * (1 << 16))()
+        n = self.L.ref_constant_image(C.cast(buf, C.c_void_p), len(buf))
+        if n <= 0:
+            raise RuntimeError(f"ref_constant_image rc={n}")
+        return bytes(buf[:n])
+
     def setup_ldpc(self, A, rate, n_iter):
         out = np.zeros(12, np.int32)
         self.L.ref_setup_ldpc(int(A), float(rate), int(n_iter), out)
@@ -317,6 +351,63 @@ class RefEmu:
         if rc:
             raise RuntimeError(f"ref_transmit_llr rc={rc}")
         return llr, info
+
+
+class RefGPU:
+    """The reference's own CUDA kernels (src/ldpc_kernels.cu compiled for the
+    GPU with nvcc's default flags into oracle/_ref/ref_kernels_bg1.cubin) run
+    on the GPU in its launch sequence by oracle/ref_gpu_harness.cpp, for its
+    own configuration: BG1, Z = 384.  Exists only where the reference tree was
+    present when oracle/_ref was built (the cubin and the constant image are
+    prebuilt there and travel with the repository copy)."""
+
+    ROWS, COLS, Z, MAX_ROW_DEG = 46, 68, 384, 19
+
+    @staticmethod
+    def available() -> bool:
+        return os.path.exists(REF_GPU_CUBIN) and os.path.exists(REF_GPU_CONST)
+
+    def __init__(self):
+        if not os.path.exists(REF_GPU_LIB):
+            subprocess.run(["make", "-C", HERE, os.path.join("_build", "libref_gpu.so")], check=True,
+                           stdout=subprocess.DEVNULL)
+        self.L = C.CDLL(REF_GPU_LIB)
+        self.L.refgpu_decode.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                         _f32p, C.c_int, C.c_int, _u8p, C.c_void_p]
+        self.L.refgpu_time.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                       _f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_float)]
+        with open(REF_GPU_CONST, "rb") as f:
+            self.image = f.read()
+        self.n_bp = self.COLS * self.Z
+
+    def decode(self, llr, n_iter, want_app=False):
+        llr = np.ascontiguousarray(llr, dtype=np.float32).reshape(-1, self.n_bp)
+        n = llr.shape[0]
+        packed = np.zeros((n, self.n_bp // 8), np.uint8)
+        app = np.zeros((n, self.n_bp), np.float32) if want_app else None
+        rc = self.L.refgpu_decode(REF_GPU_CUBIN.encode(), self.image, len(self.image), self.ROWS, self.COLS,
+                                  self.Z, self.MAX_ROW_DEG, llr, n, int(n_iter), packed, _ptr(app))
+        if rc:
+            raise RuntimeError(f"refgpu_decode rc={rc}")
+        return packed, app
+
+    def time_ms(self, llr, n_iter, warmup=3, reps=10) -> float:
+        """Mean device milliseconds of one decode of these LLRs (at most 446
+        codewords, the reference's per-stream limit), LLRs resident."""
+        llr = np.ascontiguousarray(llr, dtype=np.float32).reshape(-1, self.n_bp)
+        ms = C.c_float()
+        rc = self.L.refgpu_time(REF_GPU_CUBIN.encode(), self.image, len(self.image), self.ROWS, self.COLS, self.Z,
+                                self.MAX_ROW_DEG, llr, llr.shape[0], int(n_iter), int(warmup), int(reps),
+                                C.byref(ms))
+        if rc:
+            raise RuntimeError(f"refgpu_time rc={rc}")
+        return ms.value
+
+
+def set_fma_dt(on: bool) -> None:
+    """orc_minsum_f32 computes dt = R_new - R_old as one fused multiply-add
+    (on) or with the source's two roundings (off, the default)."""
+    lib().orc_set_fma_dt(1 if on else 0)
 
 
 # ---- code-block segmentation (3GPP TS 38.212 5.2.2), restated -----------------------

@@ -155,6 +155,35 @@ extern "C" int ref_decode(const float* llr, int n_cw, int n_iter, unsigned char*
     return 0;
 }
 
+/* The constant memory the reference's own setup writes for a decode with one
+ * codeword per block column (put_h_compact_and_params_in_constant_memory,
+ * src/setup_exp.cu:286-313, after setup_gpu_grid for n_cw_per_mcw = 1):
+ * dev_h_compact1 | dev_h_compact2 | h_element_count_per_row |
+ * h_element_count_per_col | p, as bytes, for loading into the reference's
+ * kernels built for the GPU (oracle/ref_gpu_harness.cpp).  Returns the size,
+ * or -1 before ref_init_code / when out is too small. */
+extern h_element dev_h_compact1[H_COMPACT1_COL][H_COMPACT1_ROW];
+extern h_element dev_h_compact2[H_COMPACT2_ROW][H_COMPACT2_COL];
+extern char h_element_count_per_row[BLK_ROW];
+extern char h_element_count_per_col[BLK_COL];
+extern kernel_params p[1];
+extern "C" int ref_constant_image(unsigned char* out, int cap) {
+    if (!g_ready) return -1;
+    params pr{};
+    pr.n_cw_per_mcw = 1;
+    pr.n_mcw = 1;
+    g_grid = setup_gpu_grid(&g_ldpc, 1, 1);
+    put_h_compact_and_params_in_constant_memory(&g_ldpc, &pr, &g_grid);
+    const size_t parts[5] = {sizeof(dev_h_compact1), sizeof(dev_h_compact2), sizeof(h_element_count_per_row),
+                             sizeof(h_element_count_per_col), sizeof(p)};
+    const void* srcs[5] = {dev_h_compact1, dev_h_compact2, h_element_count_per_row, h_element_count_per_col, p};
+    size_t n = 0;
+    for (size_t k : parts) n += k;
+    if (!out || (size_t)cap < n) return -1;
+    for (int i = 0, off = 0; i < 5; off += (int)parts[i], i++) std::memcpy(out + off, srcs[i], parts[i]);
+    return (int)n;
+}
+
 /* The reference's channel pipeline for BG1 A=8424 (src/setup_exp.cu:177-195):
  * srand(seed) once, then per codeword transmit (rand() info bits, OAI encoder,
  * BPSK, drand48 AWGN) and calculate_llr.  info_out: n_cw * K ints. */
