@@ -487,7 +487,51 @@ def cpu_baseline(llr_host: np.ndarray, n_sample: int, runs: int = 5):
                       f"{cores} threads, median of {runs} runs ({dt:.2f} s each; "
                       f"range {min(ts):.2f}-{max(ts):.2f} s)",
             "value_1thread": n1 * K_INFO / dt1 / 1e9,
-            "sample_1thread": f"{n1} codewords on 1 thread, median of {runs} runs ({dt1:.3f} s)"}
+            "sample_1thread": f"{n1} codewords on 1 thread, median of {runs} runs ({dt1:.3f} s)",
+            "other_configs": cpu_other_configs(runs)}
+
+
+def cpu_other_configs(runs: int = 5):
+    """The same CPU port on the other configurations of the CPU-baseline
+    plan, all host cores, median of `runs`: the reference README's workload
+    (640 codewords of the 12x24 rate-1/2 stand-in at Z=96, 5 iterations, one
+    batch per point as its SNR loop decodes) and the learned decoder of the
+    learned-vs-plain comparison (layered, weights/bg1_L6, at most 6
+    iterations, early stop, 1.8 dB) on a sample of 512 BG1 Z=384 codewords."""
+    from nr_gpu_ldpc_gb300 import codes
+    from nr_gpu_ldpc_gb300.learned import load_weights
+    from oracle.oracle import OracleCode
+    cores = os.cpu_count() or 1
+
+    def median(fn):
+        fn()  # warm
+        ts = []
+        for _ in range(runs):
+            t0 = time.perf_counter()
+            fn()
+            ts.append(time.perf_counter() - t0)
+        return statistics.median(ts)
+
+    wifi = OracleCode(codes.wifi_base(), 96)
+    k0 = 12 * 96
+    llr0, _ = wifi.gen_llr(12, 71, 0, np.full(640, codes.noise_sigma(4.0, 0.5), np.float32), 0)
+    t0 = median(lambda: wifi.minsum_f32(llr0, 5, threads=cores))
+    bg1 = OracleCode(codes.base_matrix(BG, codes.set_index(Z)), Z)
+    llr4, _ = bg1.gen_llr(22, 81, 0, np.full(512, codes.noise_sigma(1.8, K_INFO / (N_BP - 2 * Z)), np.float32), 2)
+    w = load_weights("bg1_L6")
+    res4 = {}
+
+    def run4():
+        res4["its"] = bg1.layered_f32(llr4, 6, w=w, early_stop=True, threads=cores)[2]
+    t4 = median(run4)
+    return {"c0_default_code": {"value": 640 * k0 / t0 / 1e6, "unit": "Mbit/s", "cores": cores,
+                                "sample": f"640 codewords, 12x24 Z=96 stand-in, 5 iterations, SNR 4 dB, "
+                                          f"median of {runs} runs ({1e3 * t0:.1f} ms each)"},
+            "learned_layered_bg1": {"value": 512 * K_INFO / t4 / 1e9, "unit": "Gbit/s", "cores": cores,
+                                    "avg_iters": float(res4["its"].mean()),
+                                    "sample": f"512 BG1 Z=384 codewords at 1.8 dB, layered, weights/bg1_L6, "
+                                              f"<= 6 iterations, early stop, median of {runs} runs "
+                                              f"({t4:.2f} s each)"}}
 
 
 def workload_config(batch: int) -> dict:
