@@ -93,3 +93,24 @@ def test_fp64_twin_agrees_where_fp32_is_stable():
         rel = np.abs(a32 - a64) / np.maximum(np.abs(a64), 1.0)
         assert np.quantile(rel, 0.999) < 1e-5
         assert (p32 != p64).sum() <= 2
+
+
+def test_fused_dt_switch_is_off_by_default_and_changes_posteriors(golden):
+    """The oracle's fused-dt switch (what a contracting compiler would make of
+    the reference's dt line; the reference's own binary was measured not to
+    contract it) is off unless asked for: with it on, the posteriors of a
+    BG1 Z=384 fixture differ from the reference's from the second iteration,
+    and with it off again they match."""
+    from oracle import oracle as O
+    case = next(c for c in golden["cases"] if c["code"] == "nr" and c["bg"] == 1 and c["z"] == 384
+                and "5" in c["results"] and "app_sha256" in c["results"]["5"])
+    oc, llr, _ = regen(case)
+    want = case["results"]["5"]["app_sha256"]
+    try:
+        O.set_fma_dt(True)
+        _, app_fused, _ = oc.minsum_f32(llr, 5, want_app=True)
+    finally:
+        O.set_fma_dt(False)
+    _, app, _ = oc.minsum_f32(llr, 5, want_app=True)
+    assert sha(app) == want
+    assert sha(app_fused) != want
