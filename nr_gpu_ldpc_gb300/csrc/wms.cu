@@ -87,14 +87,20 @@ __device__ __forceinline__ uint32_t edge_at(uint32_t ed, uint32_t s, uint32_t z)
 }
 
 // softplus(zz) = max(zz, 0) + log1p(e) and sigmoid(zz) = 1/(1 + e) (zz >= 0)
-// or e/(1 + e) (zz < 0), e = exp(-|zz|): one exponential per position.
-// Adds the position's loss to *loss and returns its gradient seed.
+// or e/(1 + e) (zz < 0), e = exp(-|zz|): one exponential per position, with
+// the fast hardware exponential, logarithm and division (relative errors of
+// about 1e-6, far below what the loss and its gradient are used for);
+// log1p(e) = log(u) * e / (u - 1) with u = 1 + e (Goldberg's correction:
+// u - 1 is exact, the ratio restores what rounding u lost; e itself when u
+// rounds to 1).  Adds the position's loss to *loss and returns its seed.
 __device__ __forceinline__ float loss_term(float L, bool bit1, float scale, float* loss) {
     const float y = bit1 ? -1.0f : 1.0f;
     const float zz = -y * L;
-    const float e = expf(-fabsf(zz));
-    *loss += fmaxf(zz, 0.0f) + log1pf(e);
-    const float r = __frcp_rn(1.0f + e);
+    const float e = __expf(-fabsf(zz));
+    const float u = 1.0f + e;
+    const float l1p = u == 1.0f ? e : __logf(u) * __fdividef(e, u - 1.0f);
+    *loss += fmaxf(zz, 0.0f) + l1p;
+    const float r = __fdividef(1.0f, u);
     return scale * (-y) * (zz >= 0.0f ? r : e * r);
 }
 
