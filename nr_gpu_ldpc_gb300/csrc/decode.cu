@@ -147,9 +147,12 @@ __device__ __forceinline__ uint32_t lds_u8(uint32_t a) {
 //          iteration's goes (written when store);
 //   hd:    shared byte address for the suffix column's hard decision of
 //          the posterior written (bit 1; written when sfx and write_hd).
-// Flooding reads Q = L - R_old from Lold, which holds the posterior with -0
-// made +0 (run_group's copies), so the sign bit of Q is (Q < 0) as it is;
-// Lnew and the suffix posterior in the state accumulate the exact sums.
+// Unweighted flooding (kPlain, the reference's decoder) reads Q = L - R_old
+// from Lold, which holds the posterior with -0 made +0 (run_group's copies),
+// so the sign bit of Q is (Q < 0) as it is; Lnew and the suffix posterior in
+// the state accumulate the exact sums.  The weighted and layered kernels take
+// the sign from Q + 0 and keep null addresses for the stores they skip (each
+// form measured fastest for its kernels).
 // LAYERED (no reference counterpart): one posterior buffer updated in place,
 // A = Q + R_new (dnew = 0), instead of Lnew += R_new - R_old.
 template <int D, bool WEIGHTED, bool LAYERED>
@@ -158,6 +161,7 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
                                            const float4* wprev, const float4* wcur, uint4 st, uint4* st_out,
                                            bool store, bool write_hd, uint32_t hd, float alpha) {
     constexpr int LAST = D - 1;
+    constexpr bool kPlain = !WEIGHTED && !LAYERED;
     uint32_t addr[D];
     float lv[D];
     const float sraw = __uint_as_float(st.w);  // the suffix posterior as accumulated
@@ -165,7 +169,7 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
     for (int i = 0; i < D; i++) {
         if (i == LAST && sfx) {
             addr[i] = 0;
-            lv[i] = LAYERED ? sraw : __fadd_rn(sraw, 0.0f);  // flooding: -0 read as +0, like Lold
+            lv[i] = kPlain ? __fadd_rn(sraw, 0.0f) : __uint_as_float(st.w);  // kPlain: -0 read as +0, like Lold
         } else {
             uint32_t a;
             if (LAYERED) {  // one 64-bit table read per edge (measured faster here, slower in flooding)
@@ -205,10 +209,10 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
         const float q = __fsub_rn(lv[i], ro);
         keep[i] = LAYERED ? q : ro;
         const float qa = fabsf(q);
-        // the sign bit of q is (q < 0) when q is never -0 (flooding: L is
-        // never -0, so neither is L - R_old); layered takes it from q + 0,
+        // the sign bit of q is (q < 0) when q is never -0 (kPlain: L is
+        // never -0, so neither is L - R_old); the others take it from q + 0,
         // -0 becoming +0; NaN results are canonical (+)
-        const float qs = LAYERED ? __fadd_rn(q, 0.0f) : q;
+        const float qs = kPlain ? q : __fadd_rn(q, 0.0f);
         qmask = __funnelshift_l(__float_as_uint(qs), qmask, 1);  // edge i at bit D-1-i
         if (i == 0) {  // from m1 = m2 = 1000: min2 stays 1000 whatever |Q_0| is
             m1 = fminf(m1, qa);
@@ -254,10 +258,11 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
         constexpr int kPipe = 4;
         float nv[D];
 #pragma unroll
-        for (int i = 0; i < kPipe && i < D; i++) nv[i] = (i == LAST && sfx) ? sraw : lds(addr[i] + dnew);
+        for (int i = 0; i < kPipe && i < D; i++) nv[i] = (i == LAST && sfx) ? (kPlain ? sraw : lv[i]) : lds(addr[i] + dnew);
 #pragma unroll
         for (int i = 0; i < D; i++) {
-            if (i + kPipe < D) nv[i + kPipe] = (i + kPipe == LAST && sfx) ? sraw : lds(addr[i + kPipe] + dnew);
+            if (i + kPipe < D)
+                nv[i + kPipe] = (i + kPipe == LAST && sfx) ? (kPlain ? sraw : lv[i + kPipe]) : lds(addr[i + kPipe] + dnew);
             float mag;
             if (WEIGHTED)
                 mag = __fmul_rn(wsel(wcur, i), i == idx ? m2 : m1);
@@ -272,8 +277,8 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
                 sts(addr[i] + dnew, v);
         }
     }
-    if (sfx && write_hd) sts_u8(hd, sfx_new > 0.0f ? 0u : 2u);
-    if (store) {
+    if (sfx && (kPlain ? write_hd : hd != 0u)) sts_u8(hd, sfx_new > 0.0f ? 0u : 2u);
+    if (kPlain ? store : st_out != nullptr) {
         const uint32_t info = static_cast<uint32_t>(idx) | ((rsign & ((1u << D) - 1u)) << 8);
         __stcg(st_out, make_uint4(__float_as_uint(m1), __float_as_uint(m2), info, __float_as_uint(sfx_new)));
     }
@@ -402,16 +407,20 @@ __device__ __forceinline__ void iterate_rows(const CodeTable& tab, uint32_t s, u
         if (tab.row_sfx[r]) v.w = __float_as_uint(__ldcs(gllr + edge_pos(tab, tab.row_ptr[r + 1] - 1, sj)));
         return v;
     };
-    // the state and decision addresses are always formed and the stores
-    // guarded by the flags (measured 0.8% faster than null addresses tested
-    // in the row)
+    // unweighted flooding: the state and decision addresses are always formed
+    // and the stores guarded by the flags (0.8% faster there); the other
+    // kernels get null addresses for the stores they skip (faster for them)
+    constexpr bool kPlain = !WEIGHTED && !LAYERED;
     auto run = [&](int r, uint32_t j, uint4 st) {
         const uint32_t sj = s + j * tpc;
         const bool sfx = tab.row_sfx[r] != 0;
         row_dispatch<WEIGHTED, LAYERED>(tab.row_deg[r], tab, tab.row_ptr[r], sfx, sj, s4old + 4u * j * tpc, dnew,
                                         z4, wpad + r * (kWPad / 4), wpad + (kMaxRows + r) * (kWPad / 4), st,
-                                        st_base + r * z + sj, store, write_hd,
-                                        hd_base + j * tpc + static_cast<uint32_t>(r * z), alpha);
+                                        (kPlain || store) ? st_base + r * z + sj : nullptr, store,
+                                        kPlain ? write_hd : (write_hd && sfx),
+                                        (kPlain || (write_hd && sfx)) ? hd_base + j * tpc + static_cast<uint32_t>(r * z)
+                                                                       : 0u,
+                                        alpha);
     };
     if constexpr (SPT == 1) {
         uint4 s0 = fetch(0, s), s1 = fetch(1, s);
@@ -586,13 +595,13 @@ __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slo
     const uint32_t dnew = LAYERED ? 0u : static_cast<uint32_t>(cpb) * static_cast<uint32_t>(cf) * 4u;
     const uint32_t hd_base = smem_addr(hd) + s;
     const int nt = static_cast<int>(tpc);  // threads of the slot
-    // flooding: Lnew starts as the LLRs, Lold as the LLRs with -0 made +0
-    // (the check-node pass then needs no per-edge sign fix-up)
+    // flooding: Lnew starts as the LLRs; unweighted, Lold as the LLRs with
+    // -0 made +0 (the check-node pass then needs no per-edge sign fix-up)
     if (!LAYERED && !slot_done)
         for (int k = static_cast<int>(s); k < cf / 4; k += nt) {
             const float4 v = reinterpret_cast<const float4*>(lold)[k];
             reinterpret_cast<float4*>(lnew)[k] = v;
-            reinterpret_cast<float4*>(lold)[k] = canon4(v);
+            if (!WEIGHTED) reinterpret_cast<float4*>(lold)[k] = canon4(v);
         }
     for (int t = 0; t < n_iter; t++) {
         const bool first = t == 0, last = t == n_iter - 1;
@@ -651,9 +660,10 @@ __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slo
                                   true);
             break;
         }
-        if (!LAYERED && !slot_done)  // the posterior just accumulated is the next iteration's input, -0 as +0
-            for (int k = static_cast<int>(s); k < cf / 4; k += nt)
-                reinterpret_cast<float4*>(lold)[k] = canon4(reinterpret_cast<const float4*>(lnew)[k]);
+        if (!LAYERED && !slot_done)  // the posterior just accumulated is the next iteration's input
+            for (int k = static_cast<int>(s); k < cf / 4; k += nt)  // unweighted: -0 as +0
+                reinterpret_cast<float4*>(lold)[k] = WEIGHTED ? reinterpret_cast<const float4*>(lnew)[k]
+                                                              : canon4(reinterpret_cast<const float4*>(lnew)[k]);
     }
     __syncthreads();  // buffers are rewritten by the next group's copy
     if (tid < cpb) s_far[tid] = 0;  // read again only after the next group's barriers
