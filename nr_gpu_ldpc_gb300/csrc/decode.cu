@@ -155,7 +155,7 @@ __device__ __forceinline__ uint32_t lds_u8(uint32_t a) {
 // form measured fastest for its kernels).
 // LAYERED (no reference counterpart): one posterior buffer updated in place,
 // A = Q + R_new (dnew = 0), instead of Lnew += R_new - R_old.
-template <int D, bool WEIGHTED, bool LAYERED>
+template <int D, bool WEIGHTED, bool LAYERED, bool PACKED>
 __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sfx, uint32_t s,
                                            uint32_t s4old, uint32_t dnew, uint32_t z4,
                                            const float4* wprev, const float4* wcur, uint4 st, uint4* st_out,
@@ -172,7 +172,10 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
             lv[i] = kPlain ? __fadd_rn(sraw, 0.0f) : __uint_as_float(st.w);  // kPlain: -0 read as +0, like Lold
         } else {
             uint32_t a;
-            if (LAYERED) {  // one 64-bit table read per edge (measured faster here, slower in flooding)
+            // one 64-bit table read per edge: faster for the layered kernels and
+            // for a table in shared memory (mixed batch); the single-code
+            // flooding kernels read the two words from their parameter bank
+            if (LAYERED || PACKED) {
                 const uint2 ea = tab.eaddr[e0 + i];
                 a = s4old + ea.x;
                 if (s >= ea.y) a -= z4;  // column (s + V) mod Z of the edge's block
@@ -258,11 +261,13 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
         constexpr int kPipe = 4;
         float nv[D];
 #pragma unroll
-        for (int i = 0; i < kPipe && i < D; i++) nv[i] = (i == LAST && sfx) ? (kPlain ? sraw : lv[i]) : lds(addr[i] + dnew);
+        for (int i = 0; i < kPipe && i < D; i++)
+            nv[i] = (i == LAST && sfx) ? (kPlain ? sraw : lv[i]) : lds(addr[i] + dnew);
 #pragma unroll
         for (int i = 0; i < D; i++) {
             if (i + kPipe < D)
-                nv[i + kPipe] = (i + kPipe == LAST && sfx) ? (kPlain ? sraw : lv[i + kPipe]) : lds(addr[i + kPipe] + dnew);
+                nv[i + kPipe] =
+                    (i + kPipe == LAST && sfx) ? (kPlain ? sraw : lv[i + kPipe]) : lds(addr[i + kPipe] + dnew);
             float mag;
             if (WEIGHTED)
                 mag = __fmul_rn(wsel(wcur, i), i == idx ? m2 : m1);
@@ -284,7 +289,7 @@ __device__ __forceinline__ void row_update(const CodeTable& tab, int e0, bool sf
     }
 }
 
-template <bool WEIGHTED, bool LAYERED>
+template <bool WEIGHTED, bool LAYERED, bool PACKED>
 __device__ __forceinline__ void row_dispatch(int deg, const CodeTable& tab, int e0, bool sfx, uint32_t s,
                                              uint32_t s4old, uint32_t dnew, uint32_t z4,
                                              const float4* wprev, const float4* wcur, uint4 st, uint4* st_out,
@@ -292,7 +297,7 @@ __device__ __forceinline__ void row_dispatch(int deg, const CodeTable& tab, int 
     switch (deg) {
 #define NRLDPC_ROW_CASE(D)                                                                         \
     case D:                                                                                        \
-        row_update<D, WEIGHTED, LAYERED>(tab, e0, sfx, s, s4old, dnew, z4, wprev, wcur, st, st_out, store, \
+        row_update<D, WEIGHTED, LAYERED, PACKED>(tab, e0, sfx, s, s4old, dnew, z4, wprev, wcur, st, st_out, store, \
                                          write_hd, hd, alpha);                                    \
         break;
         NRLDPC_ROW_CASE(1) NRLDPC_ROW_CASE(2) NRLDPC_ROW_CASE(3) NRLDPC_ROW_CASE(4)
@@ -392,7 +397,7 @@ __device__ __forceinline__ void write_outputs(const CodeTable& tab, const float*
 // next row's two sub-rows requested while this row's run.
 //   store: write this iteration's state; write_hd: write the suffix hard
 //   decisions.
-template <bool WEIGHTED, bool LAYERED, int SPT>
+template <bool WEIGHTED, bool LAYERED, int SPT, bool PACKED>
 __device__ __forceinline__ void iterate_rows(const CodeTable& tab, uint32_t s, uint32_t tpc, uint32_t s4old,
                                              uint32_t dnew, const float4* wpad, uint4* st_base,
                                              const float* gllr,
@@ -414,13 +419,11 @@ __device__ __forceinline__ void iterate_rows(const CodeTable& tab, uint32_t s, u
     auto run = [&](int r, uint32_t j, uint4 st) {
         const uint32_t sj = s + j * tpc;
         const bool sfx = tab.row_sfx[r] != 0;
-        row_dispatch<WEIGHTED, LAYERED>(tab.row_deg[r], tab, tab.row_ptr[r], sfx, sj, s4old + 4u * j * tpc, dnew,
-                                        z4, wpad + r * (kWPad / 4), wpad + (kMaxRows + r) * (kWPad / 4), st,
-                                        (kPlain || store) ? st_base + r * z + sj : nullptr, store,
-                                        kPlain ? write_hd : (write_hd && sfx),
-                                        (kPlain || (write_hd && sfx)) ? hd_base + j * tpc + static_cast<uint32_t>(r * z)
-                                                                       : 0u,
-                                        alpha);
+        row_dispatch<WEIGHTED, LAYERED, PACKED>(
+            tab.row_deg[r], tab, tab.row_ptr[r], sfx, sj, s4old + 4u * j * tpc, dnew, z4, wpad + r * (kWPad / 4),
+            wpad + (kMaxRows + r) * (kWPad / 4), st, (kPlain || store) ? st_base + r * z + sj : nullptr, store,
+            kPlain ? write_hd : (write_hd && sfx),
+            (kPlain || (write_hd && sfx)) ? hd_base + j * tpc + static_cast<uint32_t>(r * z) : 0u, alpha);
     };
     if constexpr (SPT == 1) {
         uint4 s0 = fetch(0, s), s1 = fetch(1, s);
@@ -451,6 +454,7 @@ __device__ __forceinline__ void iterate_rows(const CodeTable& tab, uint32_t s, u
 // of their hard-decision bytes.  Threads stop at the first failure seen by
 // any thread of the slot, so an iteration far from convergence costs a few
 // rows; *far gets the row of the failure.
+template <bool PACKED>
 __device__ __forceinline__ void check_rows(const CodeTable& tab, uint32_t s, uint32_t s4a, uint32_t hd_base,
                                            volatile int* fail, int* far) {
     const int z = tab.z;
@@ -460,8 +464,15 @@ __device__ __forceinline__ void check_rows(const CodeTable& tab, uint32_t s, uin
         const int e0 = tab.row_ptr[r], e1 = tab.row_ptr[r + 1] - (tab.row_sfx[r] ? 1 : 0);
         uint32_t par = tab.row_sfx[r] ? (lds_u8(hd_base + static_cast<uint32_t>(r * z)) >> 1) & 1u : 0u;
         for (int e = e0; e < e1; e++) {
-            uint32_t a = s4a + tab.ebase4[e];
-            if (s >= tab.ethr[e]) a -= z4;
+            uint32_t a;
+            if (PACKED) {
+                const uint2 ea = tab.eaddr[e];
+                a = s4a + ea.x;
+                if (s >= ea.y) a -= z4;
+            } else {
+                a = s4a + tab.ebase4[e];
+                if (s >= tab.ethr[e]) a -= z4;
+            }
             par ^= lds(a) > 0.0f ? 0u : 1u;
         }
         if (par) {
@@ -580,7 +591,9 @@ struct SlotOut {
 // Lold in place.  Early stop: after iteration t < n_iter - 1, a codeword
 // whose hard decisions satisfy every check stops with iters = t + 1 (the
 // oracle's rule, ldpc_oracle.c decode_one_f32).
-template <bool WEIGHTED, bool LAYERED, int SPT = 1>
+// PACKED: the table is in shared memory (the mixed batch): each edge's
+// address words come as one 64-bit read.
+template <bool WEIGHTED, bool LAYERED, int SPT = 1, bool PACKED = false>
 __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slot, uint32_t s, uint32_t tpc,
                                           bool slot_done, float* buf0, uint8_t* hd0,
                                           int* s_fail, uint4* st_base, const float* gllr, SlotOut out,
@@ -629,8 +642,8 @@ __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slo
         const bool far_check = __syncthreads_or(!slot_done && s_far[slot] >= kFarRow);
         const bool act = !slot_done;
         const bool store = !last || out.app != nullptr;
-        iterate_rows<WEIGHTED, LAYERED, SPT>(tab, s, tpc, s4old, dnew, wpad, st_base, gllr, hd_base, act, first,
-                                             store, early_stop || last, alpha);
+        iterate_rows<WEIGHTED, LAYERED, SPT, PACKED>(tab, s, tpc, s4old, dnew, wpad, st_base, gllr, hd_base, act,
+                                                     first, store, early_stop || last, alpha);
         if (early_stop && !last) {  // the rows ended with a barrier
             // bit-sliced scratch: flooding in Lold (read again only after the
             // copy-back below), layered in the weight rows (restaged at the
@@ -642,8 +655,8 @@ __device__ __forceinline__ void run_group(const CodeTable& tab, int cpb, int slo
                            s_far);
             else if (act)
                 for (int j = 0; j < SPT; j++)
-                    check_rows(tab, s + j * tpc, s4old + 4u * j * tpc + dnew, hd_base + j * tpc, &s_fail[slot],
-                               &s_far[slot]);
+                    check_rows<PACKED>(tab, s + j * tpc, s4old + 4u * j * tpc + dnew, hd_base + j * tpc,
+                                       &s_fail[slot], &s_far[slot]);
             __syncthreads();
             const bool conv = act && s_fail[slot] == 0;
             if (conv)  // HD of this iteration is a codeword
@@ -829,11 +842,11 @@ __global__ void __launch_bounds__(kMaxThreads, 2)
         uint4* st_base = reinterpret_cast<uint4*>(a.state + static_cast<size_t>(blockIdx.x) * a.slot_words) +
                          static_cast<size_t>(valid_thread ? slot : 0) * tab.rows * z;
         if (item.spt == 2)
-            run_group<false, false, 2>(tab, cpb, slot, s, static_cast<uint32_t>(tpc), !valid_thread, buf0, hd0,
+            run_group<false, false, 2, true>(tab, cpb, slot, s, static_cast<uint32_t>(tpc), !valid_thread, buf0, hd0,
                                        s_fail, st_base, a.llr + job.llr_offset, out, a.n_iter, a.early_stop, a.alpha,
                                        nullptr, nullptr, 1);
         else
-            run_group<false, false, 1>(tab, cpb, slot, s, static_cast<uint32_t>(tpc), !valid_thread, buf0, hd0,
+            run_group<false, false, 1, true>(tab, cpb, slot, s, static_cast<uint32_t>(tpc), !valid_thread, buf0, hd0,
                                        s_fail, st_base, a.llr + job.llr_offset, out, a.n_iter, a.early_stop, a.alpha,
                                        nullptr, nullptr, 1);
     }

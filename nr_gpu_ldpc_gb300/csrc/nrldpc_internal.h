@@ -43,9 +43,9 @@ struct alignas(16) CodeTable {
     uint16_t ethr[kMaxEdges];
     uint8_t edge_col[kMaxEdges];
     uint16_t edge_shift[kMaxEdges];  // V mod Z
-    // {ebase4, ethr} of each edge in one 64-bit word (the layered decoder's
-    // layout).  Last member: the mixed-batch kernel, flooding only, copies the
-    // table into shared memory up to here.
+    // {ebase4, ethr} of each edge in one 64-bit word: one read per edge for
+    // the layered decoder and for the mixed-batch kernel, which copies the
+    // whole table into shared memory
     uint2 eaddr[kMaxEdges];
 };
 
@@ -94,7 +94,7 @@ struct WorkItem {
     int32_t spt;    // sub-rows per thread: Z / spt threads per codeword (1 or 2)
 };
 constexpr size_t kHeaderBytesBatch = 1024;  // mbarrier, item id, per-slot flags
-constexpr size_t kBatchTableCopy = (offsetof(CodeTable, eaddr) + 15) / 16 * 16;
+constexpr size_t kBatchTableCopy = (sizeof(CodeTable) + 15) / 16 * 16;
 constexpr size_t kBatchTableBytes = (kBatchTableCopy + 127) / 128 * 128;
 struct BatchDecodeArgs {
     const CodeTable* tables;
