@@ -115,8 +115,9 @@ __device__ __forceinline__ void fence_proxy_async() {
 }
 
 // 32-bit shared-memory accesses by byte address.  Volatile keeps them in
-// program order; within a row every posterior load precedes every store, and
-// rows between barriers touch disjoint columns.
+// program order; a row touches each of its columns once (the load of a
+// position before its store), and rows between barriers touch disjoint
+// columns.
 __device__ __forceinline__ float lds(uint32_t a) {
     float v;
     asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(a));
