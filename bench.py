@@ -21,7 +21,10 @@ rate-matched) 8192-codeword workload in one launch; ``training`` the learned
 decoder's training step (BG2 Z=128, 8 iterations, 16384 codewords);
 ``c1_fer_curve`` the FER curve of the bench code over Eb/N0 0.5-2.5 dB;
 ``c0_default_code`` the reference README's workload (640 codewords of its
-default 12x24 rate-1/2 code, 5 iterations, SNR 0-10 dB).
+default 12x24 rate-1/2 code, 5 iterations, SNR 0-10 dB); ``testbench`` the
+reference testbench's latency and multi-stream throughput on its own
+configuration (BG1 Z=384, 5 iterations, 40-codeword batches, 6 streams, host
+buffers).
 
 Under torchrun each rank decodes its own batch (codewords are independent:
 replicas, weak scaling); rank 0 prints one JSON line with the max time over
@@ -446,6 +449,62 @@ def c0_default_code(n: int = 640, n_iter: int = 5, reps: int = 20):
                                 "(GeForce GTX 950M, its original 12x24 code)"}
 
 
+def testbench(n_cw: int = 40, n_streams: int = 6, n_iter: int = 5, reps: int = 50):
+    """The reference testbench's own two measurements (src/main.cpp:56-90,
+    125-170) on its configuration: A = 8424 info bits at rate 1/3 (BG1
+    Z=384), 5 iterations, batches of n_cw_per_mcw * n_mcw = 40 codewords per
+    stream, 6 streams, host buffers with the copies inside the timing.
+    Latency (its test_latency): one stream's batch through the host-buffer
+    call, then a device synchronize; the best and the median of `reps`.
+    Throughput (its test_throughput): every stream's batch issued back to
+    back, then one synchronize; one handle per stream (a handle serves one
+    stream at a time, as the reference's per-stream buffers do)."""
+    import torch
+    from nr_gpu_ldpc_gb300 import Decoder, codes
+    decs = [Decoder(bg=1, z=384, max_batch=n_cw) for _ in range(n_streams)]
+    streams = [torch.cuda.Stream() for _ in range(n_streams)]
+    sig = torch.full((n_cw,), codes.noise_sigma(2.0, K_INFO / (N_BP - 2 * Z)), device="cuda")
+    llr_h, out_h, want = [], [], []
+    for k, d in enumerate(decs):
+        llr, _ = d.gen_llr(seed=81, cw_base=k * n_cw, sigma=sig)
+        want.append(d.decode(llr, n_iter).cpu())
+        llr_h.append(llr.cpu().pin_memory())
+        out_h.append(torch.empty((n_cw, d.packed_bytes), dtype=torch.uint8).pin_memory())
+    torch.cuda.synchronize()
+
+    def all_streams():
+        for k, d in enumerate(decs):
+            d.decode_host(llr_h[k], out_h[k], n_iter, stream=streams[k])
+        torch.cuda.synchronize()
+
+    for _ in range(5):
+        all_streams()
+    lat, thr = [], []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        decs[0].decode_host(llr_h[0], out_h[0], n_iter, stream=streams[0])
+        torch.cuda.synchronize()
+        lat.append(time.perf_counter() - t0)
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        all_streams()
+        thr.append(time.perf_counter() - t0)
+    for k in range(n_streams):
+        assert torch.equal(out_h[k], want[k]), "host-buffer output differs from the device decode"
+    for d in decs:
+        d.close()
+    lat.sort()
+    thr.sort()
+    t_med = thr[len(thr) // 2]
+    n_all = n_cw * n_streams
+    return {"config": "BG1 Z=384 (A = 8424, rate 1/3), 5 iterations, 40 codewords per stream batch, "
+                      "6 streams, host buffers, Eb/N0 2.0 dB",
+            "best_latency_us": 1e6 * lat[0], "median_latency_us": 1e6 * lat[len(lat) // 2],
+            "throughput_ms_per_round": 1e3 * t_med, "throughput_cw_per_s": n_all / t_med,
+            "throughput_info_gbps": n_all * K_INFO / t_med / 1e9,
+            "reps": reps, "launches": reps * (1 + n_streams)}
+
+
 def cpu_model() -> str:
     """Host CPU model as lscpu names it (e.g. Neoverse-V2 on Grace)."""
     try:
@@ -589,7 +648,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling)")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain comparison")
     ap.add_argument("--no-extra", action="store_true",
-                    help="skip the mixed-batch and training legs (profiling)")
+                    help="skip the mixed-batch, training and testbench legs (profiling)")
     ap.add_argument("--batch", type=int, default=BATCH,
                     help="codewords per step (profiling a smaller launch; default 4096)")
     args = ap.parse_args()
@@ -661,7 +720,7 @@ def main():
     if not args.no_extra and rank == 0:
         for name, leg in (("mixed_batch", lambda: mixed_batch(stream)), ("training", training_step),
                           ("c1_fer_curve", lambda: c1_fer_curve(dec, min(B, 4096))),
-                          ("c0_default_code", c0_default_code)):
+                          ("c0_default_code", c0_default_code), ("testbench", testbench)):
             try:  # a failing side measurement must not cost the headline line
                 extra[name] = leg()
             except Exception as exc:  # noqa: BLE001

@@ -376,6 +376,9 @@ class RefGPU:
                                          _f32p, C.c_int, C.c_int, _u8p, C.c_void_p]
         self.L.refgpu_time.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                        _f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_float)]
+        self.L.refgpu_latency.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                          _f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_float),
+                                          C.POINTER(C.c_float)]
         with open(REF_GPU_CONST, "rb") as f:
             self.image = f.read()
         self.n_bp = self.COLS * self.Z
@@ -402,6 +405,19 @@ class RefGPU:
         if rc:
             raise RuntimeError(f"refgpu_time rc={rc}")
         return ms.value
+
+    def latency_us(self, llr, n_iter, warmup=5, reps=50):
+        """The reference testbench's latency (test_latency): host-clock
+        microseconds of one call -- H2D from pinned memory, the kernels, D2H
+        of the packed bits, synchronize -- as (best, median)."""
+        llr = np.ascontiguousarray(llr, dtype=np.float32).reshape(-1, self.n_bp)
+        best, med = C.c_float(), C.c_float()
+        rc = self.L.refgpu_latency(REF_GPU_CUBIN.encode(), self.image, len(self.image), self.ROWS, self.COLS,
+                                   self.Z, self.MAX_ROW_DEG, llr, llr.shape[0], int(n_iter), int(warmup), int(reps),
+                                   C.byref(best), C.byref(med))
+        if rc:
+            raise RuntimeError(f"refgpu_latency rc={rc}")
+        return best.value, med.value
 
 
 def set_fma_dt(on: bool) -> None:

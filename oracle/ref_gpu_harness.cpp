@@ -21,6 +21,8 @@
  */
 #include <cuda.h>
 
+#include <algorithm>
+#include <chrono>
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
@@ -220,5 +222,57 @@ extern "C" int refgpu_time(const char* cubin, const unsigned char* image, int im
     cuEventDestroy(e1);
     if (rc) return rc;
     *ms = total / reps;
+    return 0;
+}
+
+/* The reference testbench's latency measurement (test_latency,
+ * src/main.cpp:147-156) on these kernels: one perform_gpu_ldpc_decoding --
+ * H2D of the batch from pinned host memory, the launches, D2H of the packed
+ * bits into pinned host memory -- then a context synchronize, timed on the
+ * host clock (n_cw at most 446).  `warmup` untimed calls, then `reps` timed
+ * ones; the best and the median microseconds in best_us / median_us. */
+extern "C" int refgpu_latency(const char* cubin, const unsigned char* image, int image_size, int rows, int cols,
+                              int z, int max_row_deg, const float* llr, int n_cw, int n_iter, int warmup, int reps,
+                              float* best_us, float* median_us) {
+    if (!cubin || !image || !llr || !best_us || !median_us || n_cw < 1 || n_cw > 446 || n_iter < 1 || reps < 1 ||
+        z % 8 != 0)
+        return -1;
+    Ctx c;
+    RefRun k{};
+    int rc = ref_setup(c, k, cubin, image, image_size, rows, cols, z, max_row_deg, n_cw);
+    if (rc) return rc;
+    const size_t bytes = static_cast<size_t>(n_cw) * cols * z * sizeof(float);
+    const size_t out_bytes = static_cast<size_t>(n_cw) * cols * z / 8;
+    void* h_llr = nullptr;
+    void* h_out = nullptr;
+    if (cuMemAllocHost(&h_llr, bytes) != CUDA_SUCCESS) return -(__LINE__);
+    if (cuMemAllocHost(&h_out, out_bytes) != CUDA_SUCCESS) {
+        cuMemFreeHost(h_llr);
+        return -(__LINE__);
+    }
+    std::memcpy(h_llr, llr, bytes);
+    std::vector<float> us;
+    for (int i = 0; i < warmup + reps && rc == 0; i++) {
+        const auto t0 = std::chrono::steady_clock::now();
+        if (cuMemcpyHtoDAsync(k.llr, h_llr, bytes, nullptr) != CUDA_SUCCESS) {
+            rc = -(__LINE__);
+            break;
+        }
+        rc = ref_iterate(k, n_iter, nullptr);
+        if (rc) break;
+        if (cuMemcpyDtoHAsync(h_out, k.packed, out_bytes, nullptr) != CUDA_SUCCESS ||
+            cuCtxSynchronize() != CUDA_SUCCESS) {
+            rc = -(__LINE__);
+            break;
+        }
+        const auto t1 = std::chrono::steady_clock::now();
+        if (i >= warmup) us.push_back(std::chrono::duration<float, std::micro>(t1 - t0).count());
+    }
+    cuMemFreeHost(h_llr);
+    cuMemFreeHost(h_out);
+    if (rc) return rc;
+    std::sort(us.begin(), us.end());
+    *best_us = us.front();
+    *median_us = us[us.size() / 2];
     return 0;
 }
